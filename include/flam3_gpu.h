@@ -1,0 +1,260 @@
+/*
+ * flam3_gpu.h -- C ABI of the GB300 render hot path for flam3.
+ *
+ * The library (flam3_gb300/libflam3gpu.so) replaces the body of
+ * flam3_render(): chaos-game iteration, histogram accumulation, density
+ * estimation, the spatial filter and the log-density/gamma tonemap run as
+ * CUDA kernels for sm_103a; everything else about the call (arguments,
+ * output layout, error returns, consumption of the caller's ISAAC context)
+ * follows the reference.
+ *
+ * Part 1 mirrors the reference's public structs byte for byte so that a
+ * flam3_frame built by unmodified flam3 code can be handed straight to
+ * flam3gpu_render().  When the real flam3.h has already been included
+ * (flam3_included is defined) the mirror is skipped and the reference's own
+ * definitions are used.
+ *
+ * Part 2 is the drop-in entry point and its companions.
+ * Part 3 are kernel-level entry points (plain pointers and sizes) used by the
+ * parity tests and by callers that manage device memory themselves.
+ *
+ * All functions return 0 on success and nonzero on failure, with a message
+ * retrievable through flam3gpu_last_error(); none of them throws.
+ */
+#ifndef FLAM3_GPU_H
+#define FLAM3_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------
+ * Part 1: layout mirror of the reference's public structs.
+ * Field order, types and names are those of flam3.h and isaac.h; the layout
+ * has to be identical for flam3-render/flam3-animate to call this library
+ * unchanged.  The oracle build checks every offset against the real header.
+ * ---------------------------------------------------------------------- */
+#ifndef flam3_included
+
+/* isaac.h:19-31 with isaacs.h:17 (ub4 is unsigned long) */
+#define F3_RANDSIZL 4
+#define F3_RANDSIZ (1 << F3_RANDSIZL)
+typedef struct randctx {
+  unsigned long randcnt;
+  unsigned long randrsl[F3_RANDSIZ];
+  unsigned long randmem[F3_RANDSIZ];
+  unsigned long randa, randb, randc;
+} randctx;
+
+#define flam3_nvariations 99
+#define flam3_name_len 64
+#define flam3_parent_fn_len 30
+
+/* flam3.h:49-54 */
+typedef struct {
+  double index;
+  double color[4];
+} flam3_palette_entry;
+typedef flam3_palette_entry flam3_palette[256];
+
+/* flam3.h:185-191 */
+typedef struct {
+  double badvals;
+  long int num_iters;
+  int render_seconds;
+} stat_struct;
+
+/* flam3.h:213-448: one xform, variation weights and parameters */
+typedef struct xform {
+  double var[flam3_nvariations];
+  double c[3][2];
+  double post[3][2];
+  double density, color, color_speed, animate, opacity, vis_adjusted;
+  int padding;
+  double wind[2];
+  int precalc_angles_flag, precalc_atan_xy_flag, precalc_atan_yx_flag;
+  double has_preblur;
+  int has_post;
+  double blob_low, blob_high, blob_waves;
+  double pdj_a, pdj_b, pdj_c, pdj_d;
+  double fan2_x, fan2_y;
+  double rings2_val;
+  double perspective_angle, perspective_dist;
+  double julian_power, julian_dist;
+  double juliascope_power, juliascope_dist;
+  double radial_blur_angle;
+  double pie_slices, pie_rotation, pie_thickness;
+  double ngon_sides, ngon_power, ngon_circle, ngon_corners;
+  double curl_c1, curl_c2;
+  double rectangles_x, rectangles_y;
+  double amw_amp;
+  double disc2_rot, disc2_twist;
+  double super_shape_rnd, super_shape_m, super_shape_n1, super_shape_n2,
+      super_shape_n3, super_shape_holes;
+  double flower_petals, flower_holes;
+  double conic_eccentricity, conic_holes;
+  double parabola_height, parabola_width;
+  double bent2_x, bent2_y;
+  double bipolar_shift;
+  double cell_size;
+  double cpow_r, cpow_i, cpow_power;
+  double curve_xamp, curve_yamp, curve_xlength, curve_ylength;
+  double escher_beta;
+  double lazysusan_spin, lazysusan_space, lazysusan_twist, lazysusan_x, lazysusan_y;
+  double modulus_x, modulus_y;
+  double oscope_separation, oscope_frequency, oscope_amplitude, oscope_damping;
+  double popcorn2_x, popcorn2_y, popcorn2_c;
+  double separation_x, separation_xinside, separation_y, separation_yinside;
+  double split_xsize, split_ysize;
+  double splits_x, splits_y;
+  double stripes_space, stripes_warp;
+  double wedge_angle, wedge_hole, wedge_count, wedge_swirl;
+  double wedge_julia_angle, wedge_julia_count, wedge_julia_power, wedge_julia_dist;
+  double wedge_sph_angle, wedge_sph_count, wedge_sph_hole, wedge_sph_swirl;
+  double whorl_inside, whorl_outside;
+  double waves2_freqx, waves2_scalex, waves2_freqy, waves2_scaley;
+  double auger_sym, auger_weight, auger_freq, auger_scale;
+  double flux_spread;
+  double mobius_re_a, mobius_im_a, mobius_re_b, mobius_im_b;
+  double mobius_re_c, mobius_im_c, mobius_re_d, mobius_im_d;
+  /* values derived by xform_precalc (variations.c:1942-2014) */
+  double persp_vsin, persp_vfcos;
+  double julian_rN, julian_cn;
+  double juliascope_rN, juliascope_cn;
+  double wedgeJulia_rN, wedgeJulia_cn, wedgeJulia_cf;
+  double radialBlur_spinvar, radialBlur_zoomvar;
+  double waves_dx2, waves_dy2;
+  double disc2_sinadd, disc2_cosadd, disc2_timespi;
+  double super_shape_pm_4, super_shape_pneg1_n1;
+  /* active-variation list built by prepare_precalc_flags */
+  int num_active_vars;
+  double active_var_weights[flam3_nvariations];
+  int varFunc[flam3_nvariations];
+  int motion_freq, motion_func;
+  struct xform *motion;
+  int num_motion;
+} flam3_xform;
+
+/* flam3.h:450-525: a genome (control point) */
+typedef struct {
+  char flame_name[flam3_name_len + 1];
+  double time;
+  int interpolation, interpolation_type, palette_interpolation;
+  double hsv_rgb_palette_blend;
+  int num_xforms, final_xform_index, final_xform_enable;
+  flam3_xform *xform;
+  double **chaos;
+  int chaos_enable;
+  int genome_index;
+  char parent_fname[flam3_parent_fn_len];
+  int symmetry;
+  flam3_palette palette;
+  char *input_image;
+  int palette_index;
+  double brightness, contrast, gamma, highlight_power;
+  int width, height;
+  int spatial_oversample;
+  double center[2], rot_center[2];
+  double rotate, vibrancy, hue_rotation;
+  double background[3];
+  double zoom, pixels_per_unit, spatial_filter_radius;
+  int spatial_filter_select;
+  double sample_density;
+  int nbatches, ntemporal_samples;
+  double estimator, estimator_curve, estimator_minimum;
+  void *edits; /* xmlDocPtr in the reference */
+  double gam_lin_thresh;
+  int palette_index0;
+  double hue_rotation0;
+  int palette_index1;
+  double hue_rotation1, palette_blend;
+  int temporal_filter_type;
+  double temporal_filter_width, temporal_filter_exp;
+  int palette_mode;
+} flam3_genome;
+
+/* flam3.h:599-614: a render request */
+typedef struct {
+  double pixel_aspect_ratio;
+  flam3_genome *genomes;
+  int ngenomes, verbose, bits, bytes_per_channel, earlyclip;
+  double time;
+  int (*progress)(void *, double, int, double);
+  void *progress_parameter;
+  randctx rc;
+  int nthreads, sub_batch_size;
+} flam3_frame;
+
+#define flam3_field_both 0
+#define flam3_field_even 1
+#define flam3_field_odd 2
+
+#endif /* !flam3_included */
+
+/* ------------------------------------------------------------------------
+ * Part 2: drop-in render entry point.
+ * ---------------------------------------------------------------------- */
+
+/* Replaces flam3_render (flam3.h:623, flam3.c:3894-3932; body rect.c:529-1286).
+ * Same arguments and meaning: `out` is a caller-owned buffer of
+ * nchan*bytes_per_channel*width*height bytes; field selects both/even/odd
+ * scanlines; stats receives num_iters, badvals and render_seconds.  bits must
+ * be 32, 33 or 64 (else returns 1, as bits_error does).  f->rc is advanced
+ * exactly as the reference advances it (RANDSIZ draws per host thread per
+ * temporal sample), so callers that save and restore it (strips) behave the
+ * same.  The progress callback is called from the calling thread between
+ * kernel rounds with the reference's (param, percent, stage, eta) contract;
+ * a return of 1 aborts (returns 0 with a partial image), 2 pauses.
+ * Returns 0 on success, 1 on failure (message on stderr and in
+ * flam3gpu_last_error()). */
+int flam3gpu_render(flam3_frame *f, void *out, int field, int nchan, int transp, stat_struct *stats);
+
+/* Replaces flam3_render_memory_required (flam3.c:3874-3887): device bytes the
+ * render of f->genomes[0] needs (histogram + accumulator + chain state). */
+double flam3gpu_render_memory_required(flam3_frame *f);
+
+/* Last error message of the calling thread ("" if none). */
+const char *flam3gpu_last_error(void);
+
+/* Version string of the library build. */
+const char *flam3gpu_version(void);
+
+/* Execution options (no counterpart in the reference; defaults are chosen by
+ * the library).  iter_mode: 0 = one independent chain per thread, xform picked
+ * per thread (the reference's semantics); 1 = warp-coherent xform choice with
+ * a block-wide point shuffle every `shuffle_every` steps (default).  Genomes
+ * with non-unity xaos always use mode 0.  iter_precision: 32 or 64 (FP64
+ * iteration, slow on GB300; parity work).  threads_per_block, blocks: 0 =
+ * automatic.  chain_samples: samples per chain before a restart with a new
+ * random point and fuse (0 = f->sub_batch_size, like the reference). */
+typedef struct {
+  int iter_mode;
+  int iter_precision;
+  int shuffle_every;
+  int threads_per_block;
+  int blocks;
+  int chain_samples;
+  uint64_t seed_salt;
+  int reserved[8];
+} flam3gpu_options;
+
+void flam3gpu_default_options(flam3gpu_options *o);
+int flam3gpu_set_options(const flam3gpu_options *o);
+void flam3gpu_get_options(flam3gpu_options *o);
+
+/* Device-side timing of the last flam3gpu_render call on this thread, in
+ * milliseconds measured with CUDA events: [0] iterate+accumulate kernels,
+ * [1] density estimation / log scaling, [2] filter+tonemap+pack, [3] whole
+ * call wall time, [4] number of kernel launches. */
+int flam3gpu_last_timings(double t[5]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#include "flam3_gpu_kernels.h"
+
+#endif /* FLAM3_GPU_H */

@@ -1,0 +1,71 @@
+/*
+ * flam3_gpu_kernels.h -- kernel-level C ABI of libflam3gpu (plain pointers
+ * and sizes).  Included by flam3_gpu.h; see there for the drop-in entry.
+ */
+#ifndef FLAM3_GPU_KERNELS_H
+#define FLAM3_GPU_KERNELS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Optional inputs/outputs of flam3gpu_render_ex.  No counterpart in the
+ * reference: they expose the intermediate buffers of render_rectangle
+ * (rect.c:685-701) for parity checks.
+ *   hist_in  : skip iteration; every batch uses this host histogram
+ *              (hist_h rows x hist_w buckets x 5 doubles: R,G,B,A,count).
+ *   hist_out : receives the last batch's histogram in the same layout.
+ *   accum_out: receives the accumulator before the spatial filter
+ *              (hist_h x hist_w x 4 doubles).
+ *   hist_w, hist_h: set by the call. */
+typedef struct {
+  const double *hist_in;
+  double *hist_out;
+  double *accum_out;
+  int hist_w, hist_h;
+  int reserved[6];
+} flam3gpu_render_io;
+
+/* flam3gpu_render with optional parity inputs/outputs (io may be NULL). */
+int flam3gpu_render_ex(flam3_frame *f, void *out, int field, int nchan, int transp,
+                       stat_struct *stats, flam3gpu_render_io *io);
+
+/* Histogram geometry that a render of f would use (rect.c:613-687):
+ * bucket-array width/height including the gutter, gutter width, DE offset
+ * and spatial filter width. */
+int flam3gpu_histogram_dims(flam3_frame *f, int field, int *w, int *h, int *gutter,
+                            int *de_offset, int *filter_width);
+
+/* GPU apply_xform (variations.c:2129-2399) on n points: xform `fn` of genome
+ * cp (prepared on the host exactly as prepare_precalc_flags/xform_precalc
+ * do), p_in/q_out are n x 4 doubles (x, y, color, opacity) in host memory,
+ * random draws for point k are words[k*wpp ...] consumed in order, bad_out[k]
+ * receives apply_xform's return value.  precision 64 computes in FP64,
+ * precision 32 in FP32 (inputs rounded to float). */
+int flam3gpu_apply_xform(flam3_genome *cp, int fn, int n, const double *p_in,
+                         const uint32_t *words, int wpp, double *q_out, int *bad_out,
+                         int precision);
+
+/* GPU bucket accumulation (rect.c:411-516) of a host point stream
+ * (n x 4 doubles) for genome f->genomes[0] at f->time; adds into a host FP64
+ * 5-channel histogram of the render's geometry.  bits selects the device
+ * bucket type (33/32: FP32, 64: FP64). */
+int flam3gpu_accumulate_points(flam3_frame *f, int field, const double *points, long n,
+                               double *hist, int *hist_w, int *hist_h);
+
+/* GPU chaos game for parity work: nchains independent chains of flam3_iterate
+ * (flam3.c:232-299) with fuse discarded steps and n stored steps each,
+ * starting from starts[4*c..], random words from the counter-based stream
+ * keyed by `seed` (chain c uses counter (c, step/4, 0, 0) ...).  samples
+ * receives nchains x n x 4 doubles; returns the total bad-value count in
+ * *badvals. */
+int flam3gpu_iterate_chains(flam3_genome *cp, int nchains, int n, int fuse,
+                            const double *starts, uint64_t seed, double *samples,
+                            long *badvals, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
