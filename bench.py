@@ -1,0 +1,260 @@
+"""Benchmark of the flam3 render hot path on one GB300 (replicas for N>1).
+
+A step is one full render of the production-size still: a 6-xform + final
+genome with 2-4 variations each from variations 0-19, 1920x1080 output,
+quality 2000, supersample 2 (a 3878x2198 histogram incl. gutter), density
+estimation radius 9, gaussian filter radius 1, bits=33 -- 4.147 G chaos-game
+iterations, then DE + spatial filter + tonemap.  Inputs are synthetic: the
+genome comes from a seeded generator (flam3_gb300.genome.config1_genome).
+
+  value  Giter/s with the genome already on the device side of the call:
+         iterations / (sum of the render's kernel times, CUDA events on the
+         library's stream)
+  e2e    the same metric through the public C ABI flam3gpu_render with host
+         buffers: wall time of the call, which includes the host preparation,
+         the host->device copy of the pass tables and the device->host copy of
+         the image
+  roofline  for the iterate kernel (HBM view: 16 B of bucket read-modify-
+         write per plotted sample) and for the DE/filter/tonemap tail
+         (histogram read + image write)
+
+`--impl reference` times the CPU implementation of the same path on the
+host cores (the oracle build of the reference algorithm, all host threads)
+on a bounded sample of the same workload (quality reduced), same metric.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "Giter/s; renders/s and p50/p99 latency, served vs plain, at matched image error"
+WORKLOAD = "config1 still: 1920x1080 q2000 ss2 DE r9 gaussian r1, 6 xforms + final, bits 33"
+CPU_QUALITY = 100.0  # bounded CPU sample: same genome and size at quality 100 (1/20 of the iterations)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 4 + i and s[4 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(steps=1, quality=CPU_QUALITY):
+    """The oracle (plain-C restatement of the reference render path, built
+    with the reference's flags) on all host threads, on a bounded sample."""
+    import _oracle
+    from flam3_gb300 import genome as gm
+
+    _oracle.oracle(fast=True)
+    nt = cpu_threads()
+    times, iters = [], 0
+    for s in range(steps):
+        G = gm.config1_genome(1, quality=quality)
+        F = gm.Frame(G, bits=33, nthreads=nt, seed="cpu-%d" % s)
+        t0 = time.perf_counter()
+        out, st, _ = _oracle.oracle_render(F, fast=True)
+        times.append(time.perf_counter() - t0)
+        iters = st.num_iters
+    val = iters / statistics.median(times) / 1e9
+    return {"value": val, "unit": "Giter/s", "cores": nt, "kind": "port",
+            "sample": f"same genome and 1920x1080 ss2 DE9 render at quality {quality:g} "
+                      f"({iters / 1e6:.0f} M iterations) per step, median of {steps}"}, times
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        pass
+    cb, times = cpu_baseline(steps=args.steps)
+    med = statistics.median(times)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "Giter/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": med * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD + f" (CPU sample at quality {CPU_QUALITY:g})"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "Giter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def flush_l2(buf):
+    import torch
+
+    buf.add_(1)
+    torch.cuda.synchronize()
+
+
+def run_gpu(args):
+    world, rank, local = dist_setup()
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from flam3_gb300 import _build, genome as gm, render
+
+    if not os.path.exists(render._LIB_PATH):
+        _build.build()
+    render.load()
+    hbm_peak, peak_kind = peaks()
+    G = gm.config1_genome(1)
+    flush = torch.empty(320 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def one(seed):
+        F = gm.Frame(G, bits=33, seed=seed)
+        t0 = time.perf_counter()
+        img, st = render.render(F)
+        wall = time.perf_counter() - t0
+        return img, st, wall, render.last_timings()
+
+    for w in range(args.warmup):
+        one("warm-%d" % w)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    recs = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for s in range(args.steps):
+            flush_l2(flush)
+            img, st, wall, t = one("step-%d-%d" % (rank, s))
+            recs.append((st.num_iters, wall, t))
+        torch.cuda.synchronize()
+    iters = sum(r[0] for r in recs)
+    dev_s = sum((r[2]["iterate_ms"] + r[2]["de_ms"] + r[2]["tail_ms"]) / 1e3 for r in recs)
+    wall_s = sum(r[1] for r in recs)
+    it_s = sum(r[2]["iterate_ms"] / 1e3 for r in recs)
+    tail_s = sum((r[2]["de_ms"] + r[2]["tail_ms"]) / 1e3 for r in recs)
+    if world > 1:
+        t = torch.tensor([dev_s, wall_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s, wall_s = float(t[0]), float(t[1])
+        iters *= world
+    if rank != 0:
+        return
+    plotted = sum(r[2]["plotted"] for r in recs)
+    d = render.histogram_dims(gm.Frame(G, bits=33))
+    hist_bytes = d["w"] * d["h"] * 16
+    out_bytes = G.g.width * G.g.height * 3
+    it_gbs = plotted * 16 / it_s / 1e9
+    tail_gbs = args.steps * (hist_bytes + out_bytes) / tail_s / 1e9 if tail_s > 0 else None
+    value = iters / dev_s / 1e9
+    e2e = iters / wall_s / 1e9
+    cb = None
+    if world == 1 and not args.no_cpu:
+        cb, _ = cpu_baseline(steps=1)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Giter/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "iterations_per_render": recs[0][0], "renders_per_s": args.steps / dev_s,
+                   "e2e_renders_per_s": args.steps / wall_s, "l2": "flushed (320 MB write) between steps",
+                   "iterate_ms": 1e3 * it_s / args.steps, "tail_ms": 1e3 * tail_s / args.steps,
+                   "wall_ms": 1e3 * wall_s / args.steps, "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "kernel": "k_iterate", "achieved": it_gbs, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": it_gbs / hbm_peak, "traffic": None,
+                     "note": f"16 B bucket RMW per plotted sample ({plotted / args.steps / 1e9:.3f} G/render); "
+                             f"peak {peak_kind}; the kernel is issue/latency bound, not HBM bound"},
+        "roofline_tail": {"bound": "hbm", "kernel": "DE + filter + tonemap", "achieved": tail_gbs,
+                          "peak": hbm_peak, "unit": "GB/s",
+                          "frac": (tail_gbs / hbm_peak) if tail_gbs else None, "traffic": None,
+                          "note": f"histogram {hist_bytes / 1e6:.1f} MB read + image {out_bytes / 1e6:.1f} MB "
+                                  f"write per render; peak {peak_kind}"},
+        "e2e": {"value": e2e, "unit": "Giter/s", "h2d_bytes_per_step": int(recs[0][2]["h2d_bytes"]),
+                "d2h_bytes_per_step": int(recs[0][2]["d2h_bytes"])},
+        "gpu_launches": int(sum(r[2]["launches"] for r in recs)),
+        "clocks": clk.summary(),
+        "cpu_baseline": cb,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,97 @@
+"""Builds libflam3gpu.so in-tree: nvcc for the CUDA kernels (sm_103a only),
+gcc for the C host driver, translation units compiled in parallel.
+
+Usage: python -m flam3_gb300._build [--force]
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libflam3gpu.so")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + CSRC,
+                     "-I" + os.path.join(ROOT, "include")]
+CC_FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-Wall", "-Wno-unused-function", "-I" + os.path.join(ROOT, "include"),
+            "-I" + CSRC, "-I" + os.path.join(CUDA_HOME, "include")]
+
+
+def sources():
+    cu = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    c = sorted(os.path.join(CSRC, "host", f) for f in os.listdir(os.path.join(CSRC, "host")) if f.endswith(".c"))
+    return cu, c
+
+
+def headers():
+    out = []
+    for d in (CSRC, os.path.join(CSRC, "host"), os.path.join(ROOT, "include")):
+        out += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".h", ".cuh"))]
+    return out
+
+
+def _obj(src):
+    return os.path.join(BUILD, os.path.basename(src) + ".o")
+
+
+def _stale(obj, deps):
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stderr
+
+
+def build(force=False, verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    cu, c = sources()
+    hdrs = headers()
+    jobs = []
+    for s in cu:
+        o = _obj(s)
+        if force or _stale(o, [s] + hdrs):
+            jobs.append([NVCC] + NVCC_FLAGS + ["-c", s, "-o", o])
+    for s in c:
+        o = _obj(s)
+        if force or _stale(o, [s] + hdrs):
+            jobs.append(["gcc"] + CC_FLAGS + ["-c", s, "-o", o])
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
+            for msg in ex.map(_compile, jobs):
+                if verbose and msg:
+                    print(msg)
+    objs = [_obj(s) for s in cu + c]
+    if force or jobs or _stale(LIB, objs):
+        tmp = LIB + ".tmp"
+        _compile([NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread", "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def build_oracle(with_reference=None):
+    """Builds the test oracle (oracle/liboracle.so) and, where the reference
+    sources exist, oracle/_ref.  Test infrastructure only."""
+    od = os.path.join(ROOT, "oracle")
+    make = shutil.which("make")
+    subprocess.run([make, "-C", od, "port", "liboracle_fast.so"], check=True, capture_output=True)
+    ref = os.environ.get("FLAM3_REFERENCE", "/root/reference")
+    if with_reference is None:
+        with_reference = os.path.isdir(ref)
+    if with_reference:
+        subprocess.run([make, "-C", od, "ref", "REF=" + ref], check=True, capture_output=True)
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

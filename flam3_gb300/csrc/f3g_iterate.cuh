@@ -1,0 +1,423 @@
+/*
+ * f3g_iterate.cuh -- K1: chaos-game iteration + histogram accumulation.
+ *
+ * Replaces iter_thread (rect.c:253-527), flam3_iterate (flam3.c:232-299) and
+ * the bucket accumulation (rect.c:411-516).  One persistent launch processes
+ * any number of passes (temporal samples, frames, jobs): work is cut into
+ * chunks of blockDim*S samples; a block takes chunk indices from a global
+ * counter, stages the chunk's pass (xforms, variation lists, xform-choice
+ * breakpoints, colour map, camera) in shared memory, and runs fresh chains:
+ * random start point, `fuse` discarded steps, then S samples per thread.
+ *
+ * Two ways to pick xforms:
+ *   mode 0: every thread draws its own xform per step (the reference's
+ *           semantics, and the only mode for genomes with xaos);
+ *   mode 1: one draw per warp per step, so the 32 lanes run the same
+ *           variation code; every `shuffle_every` steps the block permutes
+ *           its points through shared memory so the lanes of a warp hold
+ *           points with different histories.  Each point still sees an
+ *           i.i.d. xform sequence with the genome's probabilities.
+ *
+ * Samples are added to float4 buckets with one vector atomic
+ * (red.global.add.v4.f32) or to double buckets with four FP64 atomics.
+ */
+#ifndef F3G_ITERATE_CUH
+#define F3G_ITERATE_CUH
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "f3g_common.h"
+#include "f3g_device.cuh"
+#include "f3g_launch.h"
+
+namespace f3g {
+
+template <typename R> struct PassS {
+  int num_xforms, num_std, final_index, final_enable, chaos_enable, fuse, mode, full;
+  int width, height, rotate, cmap_size, palette_mode, bucket_kind;
+  long long samples, nchunks;
+  uint32_t key0, key1;
+  R b0, b1, b2, b3, r00, r01, r10, r11, rcx, rcy, ws0, wb0s0, hs1, hb1s1;
+  double db0, db1, db2, db3, dws0, dwb0s0, dhs1, dhb1s1;
+  void *buckets, *count;
+  uint16_t nbrk[F3G_MAX_XFORMS + 1];
+  uint16_t brk[F3G_MAX_XFORMS + 1][F3G_MAX_XFORMS];
+  uint8_t var_id[F3G_MAX_VARLIST];
+  R var_w[F3G_MAX_VARLIST];
+  float4 dmap[256];
+  XfS<R> xf[F3G_MAX_XFORMS];
+};
+
+template <typename R> struct ShufPoint { R x, y, c; int consec; };
+
+/* Stage pass `p` into shared memory (all threads participate). */
+template <typename R>
+__device__ void stage_pass(PassS<R> &s, const F3GPass *__restrict__ p) {
+  const int t = threadIdx.x, T = blockDim.x;
+  if (t == 0) {
+    s.num_xforms = p->num_xforms; s.num_std = p->num_std; s.final_index = p->final_index;
+    s.final_enable = p->final_enable; s.chaos_enable = p->chaos_enable; s.fuse = p->fuse;
+    s.mode = p->iter_mode; s.full = p->full_variations;
+    s.width = p->width; s.height = p->height; s.rotate = p->rotate; s.cmap_size = p->cmap_size;
+    s.palette_mode = p->palette_mode; s.bucket_kind = p->bucket_kind;
+    s.samples = p->samples; s.nchunks = p->nchunks; s.key0 = p->key[0]; s.key1 = p->key[1];
+    s.b0 = (R)p->bounds[0]; s.b1 = (R)p->bounds[1]; s.b2 = (R)p->bounds[2]; s.b3 = (R)p->bounds[3];
+    s.db0 = p->bounds[0]; s.db1 = p->bounds[1]; s.db2 = p->bounds[2]; s.db3 = p->bounds[3];
+    s.r00 = (R)p->rot[0][0]; s.r01 = (R)p->rot[0][1]; s.r10 = (R)p->rot[1][0]; s.r11 = (R)p->rot[1][1];
+    s.rcx = (R)p->rot_center[0]; s.rcy = (R)p->rot_center[1];
+    s.ws0 = (R)p->ws0; s.wb0s0 = (R)p->wb0s0; s.hs1 = (R)p->hs1; s.hb1s1 = (R)p->hb1s1;
+    s.dws0 = p->ws0; s.dwb0s0 = p->wb0s0; s.dhs1 = p->hs1; s.dhb1s1 = p->hb1s1;
+    s.buckets = p->buckets; s.count = p->count;
+  }
+  const int nx = p->num_xforms;
+  const int rows = p->num_std + 1;
+  for (int i = t; i < rows * F3G_MAX_XFORMS; i += T) {
+    int r = i / F3G_MAX_XFORMS, c = i % F3G_MAX_XFORMS;
+    s.brk[r][c] = p->brk[r][c];
+  }
+  for (int i = t; i < rows; i += T) s.nbrk[i] = p->nbrk[i];
+  for (int i = t; i < F3G_MAX_VARLIST; i += T) {
+    s.var_id[i] = p->var_id[i];
+    s.var_w[i] = (R)p->var_w[i];
+  }
+  for (int i = t; i < 256; i += T)
+    s.dmap[i] = make_float4(p->dmap[i][0], p->dmap[i][1], p->dmap[i][2], p->dmap[i][3]);
+  /* xform scalars and parameters */
+  const int per = 6 + 6 + 5 + PRM_COUNT;
+  for (int i = t; i < nx * per; i += T) {
+    int xi = i / per, k = i % per;
+    const F3GXform &g = p->xf[xi];
+    XfS<R> &d = s.xf[xi];
+    if (k < 6) d.c[k] = (R)g.c[k];
+    else if (k < 12) d.post[k - 6] = (R)g.post[k - 6];
+    else if (k == 12) d.color = (R)g.color;
+    else if (k == 13) d.color_speed = (R)g.color_speed;
+    else if (k == 14) d.vis_adjusted = (R)g.vis_adjusted;
+    else if (k == 15) d.opacity = (R)g.opacity;
+    else if (k == 16) {
+      d.preblur = (R)g.preblur;
+      d.flags = g.flags;
+      d.var_off = g.var_off;
+      d.nvars = g.nvars;
+    } else
+      d.prm[k - 17] = (R)g.prm[k - 17];
+  }
+}
+
+/* xform choice: the number of breakpoints of row `row` that are <= v */
+template <typename R>
+__device__ __forceinline__ int pick_xform(const PassS<R> &s, int row, uint32_t v) {
+  int n = s.nbrk[row], fn = 0;
+  for (int k = 0; k < n; k++) fn += (s.brk[row][k] <= v);
+  return fn;
+}
+
+/* rect.c:411-516 for one sample */
+template <typename R>
+__device__ __forceinline__ unsigned plot(const PassS<R> &s, R qx, R qy, R qc, R qo) {
+  R p0 = qx, p1 = qy;
+  if (s.rotate) {
+    R p00 = qx - s.rcx, p11 = qy - s.rcy;
+    p0 = p00 * s.r00 + p11 * s.r01 + s.rcx;
+    p1 = p00 * s.r10 + p11 * s.r11 + s.rcy;
+  }
+  if (!(p0 >= s.b0 && p1 >= s.b1 && p0 <= s.b2 && p1 <= s.b3)) return 0u;
+  if (qo == (R)0) return 0u;
+  int xi, yi;
+  if (sizeof(R) == 8) {
+    xi = (int)(s.dws0 * (double)p0 - s.dwb0s0);
+    yi = (int)(s.dhs1 * (double)p1 - s.dhb1s1);
+  } else {
+    /* same index as the reference's ws0*p0 - wb0s0, rearranged so FP32 does
+     * not cancel against a large wb0s0 */
+    xi = (int)(s.ws0 * (p0 - s.b0));
+    yi = (int)(s.hs1 * (p1 - s.b1));
+  }
+  long long idx = (long long)xi + (long long)s.width * yi;
+  if (idx < 0 || idx >= (long long)s.width * s.height) return 0u;
+  float4 col;
+  const R dbl_index0 = qc * (R)s.cmap_size;
+  int ci = (int)dbl_index0;
+  const int cm1 = s.cmap_size - 1;
+  if (s.palette_mode == 1) {
+    R frac;
+    if (ci < 0) { ci = 0; frac = (R)0; }
+    else if (ci >= cm1) { ci = cm1 - 1; frac = (R)1; }
+    else frac = dbl_index0 - (R)ci;
+    float4 a = s.dmap[ci], b = s.dmap[ci + 1];
+    float ff = (float)frac, gg = 1.0f - ff;
+    col = make_float4(a.x * gg + b.x * ff, a.y * gg + b.y * ff, a.z * gg + b.z * ff, a.w * gg + b.w * ff);
+  } else {
+    if (ci < 0) ci = 0;
+    else if (ci >= cm1) ci = cm1;
+    col = s.dmap[ci];
+  }
+  float cnt = 255.0f;
+  if (qo != (R)1) {
+    float o = (float)qo;
+    col.x *= o; col.y *= o; col.z *= o; col.w *= o;
+    cnt *= o;
+  }
+  if (s.bucket_kind == F3G_BK_F32) {
+    float4 *b = (float4 *)s.buckets + idx;
+    atomicAdd(b, col);
+    if (s.count) atomicAdd((float *)s.count + idx, cnt);
+  } else {
+    double *b = (double *)s.buckets + 4 * idx;
+    atomicAdd(b + 0, (double)col.x);
+    atomicAdd(b + 1, (double)col.y);
+    atomicAdd(b + 2, (double)col.z);
+    atomicAdd(b + 3, (double)col.w);
+    if (s.count) atomicAdd((double *)s.count + idx, (double)cnt);
+  }
+  return 1u;
+}
+
+/* One chain step (flam3.c:249-296).  Returns true when q is a sample to
+ * store (false while retrying a bad value). */
+template <typename R, bool FULL, class G>
+__device__ __forceinline__ bool chain_step(const PassS<R> &s, int fn, R &px, R &py, R &pc, R &po, int &consec,
+                                           int &lastxf, unsigned &bad, R &qx, R &qy, R &qc, R &qo, G &rng) {
+  const XfS<R> &x = s.xf[fn];
+  R nx, ny, nc, no;
+  if (apply_xform<R, FULL, G>(x, s.var_id, s.var_w, px, py, pc, nx, ny, nc, no, rng)) {
+    consec++;
+    bad++;
+    if (consec < 5) {
+      px = nx; py = ny; pc = nc; po = no;
+      return false;
+    }
+    consec = 0;
+  } else
+    consec = 0;
+  lastxf = fn + 1;
+  px = nx; py = ny; pc = nc; po = no;
+  qx = px; qy = py; qc = pc; qo = po;
+  if (s.final_enable) {
+    const XfS<R> &fx = s.xf[s.final_index];
+    if (fx.opacity == (R)1 || u01<R>(rng.word()) < fx.opacity) {
+      R fo;
+      apply_xform<R, FULL, G>(fx, s.var_id, s.var_w, px, py, pc, qx, qy, qc, fo, rng);
+      qo = po;
+    }
+  }
+  return true;
+}
+
+/* mode 0: independent chains, one per thread */
+template <typename R, bool FULL>
+__device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, int S, unsigned &bad_total,
+                                 unsigned &hits) {
+  const int T = blockDim.x, t = threadIdx.x;
+  long long base = local_chunk * (long long)T * S;
+  long long n_chunk = s.samples - base;
+  if (n_chunk > (long long)T * S) n_chunk = (long long)T * S;
+  long long q = n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0);
+  Rng rng;
+  rng.init(s.key0, s.key1, (uint32_t)local_chunk, (uint32_t)t, 0x5EEDu);
+  R px = u11<R>(rng.word()), py = u11<R>(rng.word()), pc = u01<R>(rng.word()), po = u01<R>(rng.word());
+  int consec = 0, lastxf = 0;
+  unsigned bad = 0;
+  const int total = s.fuse;
+  for (long long i = -total; i < q;) {
+    int row = s.chaos_enable ? min(lastxf, s.num_std) : 0;
+    int fn = pick_xform(s, row, rng.word() & (F3G_GRAIN - 1));
+    R qx, qy, qc, qo;
+    if (!chain_step<R, FULL, Rng>(s, fn, px, py, pc, po, consec, lastxf, bad, qx, qy, qc, qo, rng)) continue;
+    if (i >= 0) hits += plot(s, qx, qy, qc, qo);
+    i++;
+  }
+  bad_total += bad;
+}
+
+/* mode 1: warp-coherent xform choice plus block-wide point shuffles */
+template <typename R, bool FULL>
+__device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long local_chunk, int S, int shuffle_every,
+                               unsigned &bad_total, unsigned &hits) {
+  const int T = blockDim.x, t = threadIdx.x, lane = t & 31, nwarps = T >> 5;
+  long long base = local_chunk * (long long)T * S;
+  long long n_chunk = s.samples - base;
+  if (n_chunk > (long long)T * S) n_chunk = (long long)T * S;
+  long long q = n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0);
+  Rng rng;
+  rng.init(s.key0, s.key1, (uint32_t)local_chunk, (uint32_t)t, 0x5EEDu);
+  R px = u11<R>(rng.word()), py = u11<R>(rng.word()), pc = u01<R>(rng.word()), po = u01<R>(rng.word());
+  int consec = 0, lastxf = 0;
+  unsigned bad = 0;
+  /* fuse, then sample; the block leaves only when every thread is done */
+  int fuse_left = s.fuse;
+  long long remaining = q;
+  uint32_t rot = 0;
+  for (int round = 0;; round++) {
+    for (int k = 0; k < shuffle_every; k++) {
+      uint32_t w = __shfl_sync(0xffffffffu, rng.word(), 0);
+      int fn = pick_xform(s, 0, w & (F3G_GRAIN - 1));
+      R qx, qy, qc, qo;
+      bool ok = chain_step<R, FULL, Rng>(s, fn, px, py, pc, po, consec, lastxf, bad, qx, qy, qc, qo, rng);
+      if (ok) {
+        if (fuse_left > 0) fuse_left--;
+        else if (remaining > 0) {
+          hits += plot(s, qx, qy, qc, qo);
+          remaining--;
+        }
+      }
+    }
+    rot += 0x9E3779B1u * (uint32_t)(round + 1);
+    /* transpose lanes across warps, then rotate by a block-uniform amount */
+    int dst = ((lane * nwarps + (t >> 5)) + (int)(rot >> 20)) & (T - 1);
+    __syncthreads();
+    buf[dst].x = px; buf[dst].y = py; buf[dst].c = pc; buf[dst].consec = consec;
+    int more = __syncthreads_or(remaining > 0 || fuse_left > 0);
+    px = buf[t].x; py = buf[t].y; pc = buf[t].c; consec = buf[t].consec;
+    if (!more) break;
+  }
+  (void)po;
+  bad_total += bad;
+}
+
+template <typename R, bool FULL>
+__global__ void __launch_bounds__(256) k_iterate(const F3GPass *__restrict__ passes,
+                                                 const long long *__restrict__ chunk_prefix, int npasses,
+                                                 long long total_chunks, int S, int shuffle_every,
+                                                 F3GCounters *ctr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PassS<R> &s = *reinterpret_cast<PassS<R> *>(smem_raw);
+  ShufPoint<R> *buf = reinterpret_cast<ShufPoint<R> *>(smem_raw + ((sizeof(PassS<R>) + 15) & ~(size_t)15));
+  __shared__ long long sh_chunk;
+  __shared__ int sh_pass;
+  int cur = -1;
+  unsigned bad = 0, hits = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      long long g = (long long)atomicAdd(&ctr->next_chunk, 1ull);
+      int p = cur;
+      if (g < total_chunks) {
+        if (p < 0 || g < chunk_prefix[p] || g >= chunk_prefix[p + 1]) {
+          int lo = 0, hi = npasses - 1;
+          while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (chunk_prefix[mid] <= g) lo = mid;
+            else hi = mid - 1;
+          }
+          p = lo;
+        }
+      }
+      sh_chunk = g;
+      sh_pass = p;
+    }
+    __syncthreads();
+    long long g = sh_chunk;
+    int p = sh_pass;
+    if (g >= total_chunks) break;
+    if (p != cur) {
+      stage_pass<R>(s, passes + p);
+      cur = p;
+      __syncthreads();
+    }
+    long long local = g - chunk_prefix[p];
+    if (s.mode == 1) run_chunk_warp<R, FULL>(s, buf, local, S, shuffle_every, bad, hits);
+    else run_chunk_thread<R, FULL>(s, local, S, bad, hits);
+    __syncthreads();
+  }
+  /* badvals: warp reduce then one atomic per warp */
+  unsigned long long h = hits;
+  for (int o = 16; o > 0; o >>= 1) {
+    bad += __shfl_down_sync(0xffffffffu, bad, o);
+    h += __shfl_down_sync(0xffffffffu, h, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (bad) atomicAdd(&ctr->badvals, (unsigned long long)bad);
+    if (h) atomicAdd(&ctr->plotted, h);
+  }
+}
+
+template <typename R, bool FULL> static size_t iterate_smem(int threads) {
+  return ((sizeof(PassS<R>) + 15) & ~(size_t)15) + sizeof(ShufPoint<R>) * (size_t)threads;
+}
+
+template <typename R, bool FULL>
+static cudaError_t launch_iterate_t(const F3GPass *d_passes, const long long *d_prefix, int npasses,
+                                    long long total_chunks, int S, int shuffle_every, int threads, int blocks,
+                                    F3GCounters *d_ctr, cudaStream_t st) {
+  size_t smem = iterate_smem<R, FULL>(threads);
+  cudaError_t e = cudaFuncSetAttribute(k_iterate<R, FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_iterate<R, FULL><<<blocks, threads, smem, st>>>(d_passes, d_prefix, npasses, total_chunks, S, shuffle_every,
+                                                    d_ctr);
+  return cudaGetLastError();
+}
+
+}  // namespace f3g
+
+/* ---------------------------------------------------------------------
+ * Parity probes: apply_xform on given points/words, accumulation of a given
+ * point stream, and chains with recorded output.  One block stages the pass;
+ * grids are small (test sizes).
+ * ------------------------------------------------------------------- */
+namespace f3g {
+
+template <typename R, bool FULL>
+__global__ void __launch_bounds__(256) k_apply_xform(const F3GPass *__restrict__ pass, int fn, int n,
+                                                     const double *__restrict__ pin,
+                                                     const uint32_t *__restrict__ words, int wpp, double *qout,
+                                                     int *bad) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PassS<R> &s = *reinterpret_cast<PassS<R> *>(smem_raw);
+  stage_pass<R>(s, pass);
+  __syncthreads();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    ArrayRng rng{words + (size_t)k * wpp, wpp, 0};
+    R qx, qy, qc, qo;
+    bool b = apply_xform<R, FULL, ArrayRng>(s.xf[fn], s.var_id, s.var_w, (R)pin[4 * k], (R)pin[4 * k + 1],
+                                            (R)pin[4 * k + 2], qx, qy, qc, qo, rng);
+    qout[4 * k] = (double)qx;
+    qout[4 * k + 1] = (double)qy;
+    qout[4 * k + 2] = (double)qc;
+    qout[4 * k + 3] = (double)qo;
+    bad[k] = b ? 1 : 0;
+  }
+}
+
+static __global__ void __launch_bounds__(256) k_accumulate(const F3GPass *__restrict__ pass, const double *__restrict__ pts,
+                                                    long long n) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PassS<double> &s = *reinterpret_cast<PassS<double> *>(smem_raw);
+  stage_pass<double>(s, pass);
+  __syncthreads();
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    (void)plot<double>(s, pts[4 * k], pts[4 * k + 1], pts[4 * k + 2], pts[4 * k + 3]);
+}
+
+template <typename R, bool FULL>
+__global__ void __launch_bounds__(256) k_iterate_chains(const F3GPass *__restrict__ pass, int nchains, int n,
+                                                        int fuse, const double *__restrict__ starts, uint32_t key0,
+                                                        uint32_t key1, double *samples, unsigned long long *bad_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PassS<R> &s = *reinterpret_cast<PassS<R> *>(smem_raw);
+  stage_pass<R>(s, pass);
+  __syncthreads();
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nchains) return;
+  Rng rng;
+  rng.init(key0, key1, (uint32_t)c, 0u, 0xC4A1u);
+  R px = (R)starts[4 * c], py = (R)starts[4 * c + 1], pc = (R)starts[4 * c + 2], po = (R)starts[4 * c + 3];
+  int consec = 0, lastxf = 0;
+  unsigned bad = 0;
+  for (int i = -fuse; i < n;) {
+    int row = s.chaos_enable ? min(lastxf, s.num_std) : 0;
+    int fn = pick_xform(s, row, rng.word() & (F3G_GRAIN - 1));
+    R qx, qy, qc, qo;
+    if (!chain_step<R, FULL, Rng>(s, fn, px, py, pc, po, consec, lastxf, bad, qx, qy, qc, qo, rng)) continue;
+    if (i >= 0) {
+      double *o = samples + ((size_t)c * n + i) * 4;
+      o[0] = (double)qx; o[1] = (double)qy; o[2] = (double)qc; o[3] = (double)qo;
+    }
+    i++;
+  }
+  atomicAdd(bad_out, (unsigned long long)bad);
+}
+
+}  // namespace f3g
+
+
+#endif

@@ -1,0 +1,57 @@
+/*
+ * f3g_launch.h -- internal C interface between the host driver and the
+ * kernel launch wrappers (all return a cudaError_t value, 0 on success).
+ */
+#ifndef F3G_LAUNCH_H
+#define F3G_LAUNCH_H
+
+#include <cuda_runtime.h>
+
+#include "f3g_common.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* tonemap constants of one render (rect.c:1069-1081) */
+typedef struct {
+  float g;            /* 1 / mean gamma */
+  float linrange;     /* gam_lin_thresh */
+  float funcval;      /* linrange^g */
+  float vibrancy;     /* mean vibrancy */
+  float highpow;      /* highlight_power */
+  float background[3];/* mean background * 256 */
+  int nchan, transp, bpc;
+} F3GTonemap;
+
+int f3g_iterate_occupancy(int precision, int full, int threads);
+int f3g_launch_iterate(const F3GPass *d_passes, const long long *d_prefix, int npasses, long long total_chunks,
+                       int S, int shuffle_every, int precision, int full, int threads, int blocks,
+                       F3GCounters *d_ctr, cudaStream_t st);
+
+int f3g_launch_logscale(const void *buckets, int bkind, long long n, double k1, double k2, void *acc, int akind,
+                        cudaStream_t st);
+int f3g_launch_de(const void *buckets, int bkind, const void *count, int W, int H, int oversample, double k1,
+                  double k2, double curve, int max_filtered_counts, int max_filter_index, int kernel_size,
+                  const float *widths, const float *coefs, int R, void *acc, int akind, cudaStream_t st);
+int f3g_de_max_reach(void);
+int f3g_launch_earlyclip(void *acc, int akind, long long n, const F3GTonemap *tp, cudaStream_t st);
+int f3g_launch_filter_tonemap(const void *acc, int akind, int W, int de_offset, int oversample, const float *filter,
+                              int fw, int image_w, int image_h, unsigned char *out, int earlyclip,
+                              const F3GTonemap *tp, cudaStream_t st);
+int f3g_launch_fused_log_filter(const void *buckets, int bkind, int W, int H, double k1, double k2, int de_offset,
+                                int oversample, const float *filter, int fw, int image_w, int image_h,
+                                unsigned char *out, int earlyclip, const F3GTonemap *tp, cudaStream_t st);
+
+/* parity helpers (f3g_probe.cu) */
+int f3g_launch_apply_xform(const F3GPass *d_pass, int fn, int n, const double *d_pin, const uint32_t *d_words,
+                           int wpp, double *d_qout, int *d_bad, int precision, cudaStream_t st);
+int f3g_launch_accumulate(const F3GPass *d_pass, const double *d_points, long long n, cudaStream_t st);
+int f3g_launch_iterate_chains(const F3GPass *d_pass, int nchains, int n, int fuse, const double *d_starts,
+                              uint32_t key0, uint32_t key1, double *d_samples, unsigned long long *d_bad,
+                              int precision, cudaStream_t st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,76 @@
+/*
+ * f3g_host.h -- internal interface of the libflam3gpu host driver (C).
+ */
+#ifndef F3G_HOST_H
+#define F3G_HOST_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "flam3_gpu.h"
+#include "../f3g_common.h"
+#include "../f3g_launch.h"
+
+#ifndef F3_RANDSIZ
+#define F3_RANDSIZ RANDSIZ
+#endif
+
+/* error reporting: message kept per thread, also printed to stderr */
+void f3g_set_error(const char *fmt, ...);
+void f3g_clear_error(void);
+
+#define F3G_CUDA(call)                                                            \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) {                                                      \
+      f3g_set_error("CUDA error %s at %s:%d", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return 1;                                                                   \
+    }                                                                             \
+  } while (0)
+
+/* ---- genome preparation (prep.c) ---- */
+void f3g_genome_free(flam3_genome *g);
+void f3g_genome_copy(flam3_genome *dst, const flam3_genome *src);
+int f3g_interpolate(flam3_genome *cps, int ncps, double time, flam3_genome *result);
+int f3g_prepare_precalc_flags(flam3_genome *cp);
+void f3g_xform_precalc(flam3_genome *cp, int xi);
+/* builds the xform-choice table rows (flam3.c:76-224) and stores them as
+ * breakpoints into pass; returns 0 on success */
+int f3g_build_distrib(flam3_genome *cp, F3GPass *pass);
+/* fills the genome part of a pass from a prepared genome */
+int f3g_pack_genome(flam3_genome *cp, F3GPass *pass);
+
+/* ---- filters (filters.c) ---- */
+int f3g_spatial_filter(flam3_frame *spec, int field, double **filter);
+int f3g_de_filters(double max_rad, double min_rad, double curve, int ss, int *max_filtered_counts,
+                   int *max_filter_index, double **widths, double **coefs);
+double f3g_temporal_filter(int numsteps, int filter_type, double filter_exp, double filter_width, double **tfilter,
+                           double **tdeltas);
+
+/* ---- per-thread device context (render.c) ---- */
+typedef struct {
+  int device, nsm, ready;
+  cudaStream_t stream;
+  cudaEvent_t ev[8];
+  void *d_hist; size_t hist_bytes;
+  void *d_count; size_t count_bytes;
+  void *d_acc; size_t acc_bytes;
+  unsigned char *d_out; size_t out_bytes;
+  F3GPass *d_passes; size_t passes_bytes;
+  F3GPass *h_passes; size_t h_passes_bytes; /* pinned */
+  long long *d_prefix; size_t prefix_bytes; long long *h_prefix; size_t prefix_n;
+  F3GCounters *d_ctr; F3GCounters *h_ctr;
+  float *d_filter; size_t filter_bytes;
+  float *d_de_w; size_t de_w_bytes;
+  float *d_de_c; size_t de_c_bytes;
+  double timings[8];
+} f3g_ctx;
+
+f3g_ctx *f3g_get_ctx(void);
+int ensure_host_pass_one(f3g_ctx *c);
+int f3g_ensure(void **ptr, size_t *cap, size_t need);
+extern flam3gpu_options f3g_opts;
+/* samples per thread per chunk for a pass of `samples` samples */
+int f3g_chunk_samples(const f3g_ctx *c, long long samples, int threads, int blocks, int sub_batch_size);
+
+#endif

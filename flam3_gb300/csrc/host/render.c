@@ -1,0 +1,755 @@
+/*
+ * render.c -- flam3gpu_render: the GPU body of flam3_render.
+ *
+ * Follows render_rectangle (rect.c:529-1286) step for step on the host --
+ * interpolation, filters, gutter, batches, temporal samples, camera, k1/k2,
+ * tonemap constants, consumption of the caller's ISAAC context -- and runs
+ * the per-pixel and per-sample work as kernels:
+ *
+ *   iterate (all temporal samples of a batch in one persistent launch)
+ *   -> [one batch, no DE]  fused log-scale + filter + tonemap + pack
+ *   -> [otherwise]         log-scale or DE into the accumulator per batch,
+ *                          then earlyclip / filter + tonemap + pack
+ *
+ * Device buffers live in a per-thread context and are reused across calls.
+ */
+#define _GNU_SOURCE
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "f3g_host.h"
+
+#define F3G_WHITE 255.0
+
+static __thread f3g_ctx tls_ctx;
+
+/* CUDA call inside flam3gpu_render_ex: record the error and leave through `done` */
+#define CK(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      f3g_set_error("CUDA error %s at %s:%d", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      goto done;                                                                           \
+    }                                                                                      \
+  } while (0)
+
+f3g_ctx *f3g_get_ctx(void) {
+  f3g_ctx *c = &tls_ctx;
+  if (!c->ready) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return NULL;
+    c->device = dev;
+    if (cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return NULL;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return NULL;
+    for (int i = 0; i < 8; i++)
+      if (cudaEventCreate(&c->ev[i]) != cudaSuccess) return NULL;
+    if (cudaMalloc((void **)&c->d_ctr, sizeof(F3GCounters)) != cudaSuccess) return NULL;
+    if (cudaMallocHost((void **)&c->h_ctr, sizeof(F3GCounters)) != cudaSuccess) return NULL;
+    c->ready = 1;
+  }
+  return c;
+}
+
+int f3g_ensure(void **ptr, size_t *cap, size_t need) {
+  if (need <= *cap && *ptr) return 0;
+  if (*ptr) cudaFree(*ptr);
+  *ptr = NULL;
+  *cap = 0;
+  size_t alloc = need < 256 ? 256 : need;
+  cudaError_t e = cudaMalloc(ptr, alloc);
+  if (e != cudaSuccess) {
+    f3g_set_error("cudaMalloc of %zu bytes failed: %s", alloc, cudaGetErrorString(e));
+    *ptr = NULL;
+    return 1;
+  }
+  *cap = alloc;
+  return 0;
+}
+
+static int ensure_host_passes(f3g_ctx *c, size_t n) {
+  size_t need = n * sizeof(F3GPass);
+  if (need <= c->h_passes_bytes && c->h_passes) return 0;
+  if (c->h_passes) cudaFreeHost(c->h_passes);
+  c->h_passes = NULL;
+  if (cudaMallocHost((void **)&c->h_passes, need) != cudaSuccess) {
+    f3g_set_error("cudaMallocHost of %zu bytes failed", need);
+    c->h_passes_bytes = 0;
+    return 1;
+  }
+  c->h_passes_bytes = need;
+  if (c->h_prefix) cudaFreeHost(c->h_prefix);
+  if (cudaMallocHost((void **)&c->h_prefix, (n + 1) * sizeof(long long)) != cudaSuccess) return 1;
+  c->prefix_n = n + 1;
+  return 0;
+}
+
+int f3g_chunk_samples(const f3g_ctx *c, long long samples, int threads, int blocks, int sub_batch_size) {
+  (void)c;
+  long long per = samples / ((long long)threads * blocks);
+  int cap = f3g_opts.chain_samples > 0 ? f3g_opts.chain_samples : 1024;
+  if (sub_batch_size > 0 && cap > sub_batch_size) cap = sub_batch_size;
+  if (per > cap) per = cap;
+  if (per < 64) per = 64;
+  if (per > cap) per = cap;
+  return (int)per;
+}
+
+/* geometry of a render (rect.c:613-687) */
+typedef struct {
+  int oversample, image_width, image_height, out_width;
+  int filter_width, gutter, de_offset, W, H;
+} f3g_geom;
+
+static int compute_geom(flam3_frame *spec, const flam3_genome *cp, int field, double **filter, f3g_geom *g) {
+  g->oversample = cp->spatial_oversample;
+  g->image_width = cp->width;
+  g->out_width = g->image_width;
+  if (field) {
+    g->image_height = cp->height / 2;
+    g->out_width *= 2;
+  } else
+    g->image_height = cp->height;
+  double *flt = NULL;
+  g->filter_width = f3g_spatial_filter(spec, field, &flt);
+  if (g->filter_width < 0) return 1;
+  if (filter) *filter = flt;
+  else free(flt);
+  g->gutter = (g->filter_width - g->oversample) / 2;
+  int mx = 0;
+  for (int i = 0; i < spec->ngenomes; i++) {
+    int w = (int)ceil(spec->genomes[i].estimator) * g->oversample;
+    if (w > mx) mx = w;
+  }
+  if (mx > 0) mx += g->oversample - 1;
+  if (mx > g->gutter) {
+    g->de_offset = mx - g->gutter;
+    g->gutter = mx;
+  } else
+    g->de_offset = 0;
+  g->H = g->oversample * g->image_height + 2 * g->gutter;
+  g->W = g->oversample * g->image_width + 2 * g->gutter;
+  return 0;
+}
+
+/* camera of one temporal sample (rect.c:785-827) */
+static int set_camera(flam3_frame *spec, const flam3_genome *cp, int field, const f3g_geom *g, F3GPass *p,
+                      double *sample_density, double *ppux_out, double *ppuy_out) {
+  if (cp->sample_density <= 0.0) {
+    f3g_set_error("sample density (quality) must be greater than zero, not %g.", cp->sample_density);
+    return 1;
+  }
+  double scale = pow(2.0, cp->zoom);
+  *sample_density = cp->sample_density * scale * scale;
+  double ppux = cp->pixels_per_unit * scale, ppuy = field ? ppux / 2.0 : ppux, shift = 0.0;
+  ppux /= spec->pixel_aspect_ratio;
+  if (field == flam3_field_even) shift = -0.5;
+  else if (field == flam3_field_odd) shift = 0.5;
+  shift = shift / ppux;
+  double t0 = (double)g->gutter / (g->oversample * ppux), t1 = (double)g->gutter / (g->oversample * ppuy);
+  double corner0 = cp->center[0] - g->image_width / ppux / 2.0;
+  double corner1 = cp->center[1] - g->image_height / ppuy / 2.0;
+  p->bounds[0] = corner0 - t0;
+  p->bounds[1] = corner1 - t1 + shift;
+  p->bounds[2] = corner0 + g->image_width / ppux + t0;
+  p->bounds[3] = corner1 + g->image_height / ppuy + t1 + shift;
+  double size0 = 1.0 / (p->bounds[2] - p->bounds[0]), size1 = 1.0 / (p->bounds[3] - p->bounds[1]);
+  p->rot[0][0] = cos(cp->rotate * 2 * M_PI / 360.0);
+  p->rot[0][1] = -sin(cp->rotate * 2 * M_PI / 360.0);
+  p->rot[1][0] = -p->rot[0][1];
+  p->rot[1][1] = p->rot[0][0];
+  p->rot_center[0] = cp->rot_center[0];
+  p->rot_center[1] = cp->rot_center[1];
+  p->rotate = cp->rotate != 0.0;
+  p->width = g->W;
+  p->height = g->H;
+  p->ws0 = g->W * size0;
+  p->wb0s0 = p->ws0 * p->bounds[0];
+  p->hs1 = g->H * size1;
+  p->hb1s1 = p->hs1 * p->bounds[1];
+  *ppux_out = ppux;
+  *ppuy_out = ppuy;
+  return 0;
+}
+
+static unsigned long irand(randctx *r);
+
+/* Advance the caller's ISAAC context as the reference does for one temporal
+ * sample (rect.c:858-865: RANDSIZ words per host thread) and derive the
+ * pass's Philox key from the words drawn. */
+static void consume_rc(flam3_frame *spec, uint32_t key[2]) {
+  int nthreads = spec->nthreads < 1 ? 1 : spec->nthreads;
+  uint32_t w[4] = {0, 0, 0, 0};
+  for (int t = 0; t < nthreads; t++)
+    for (int k = 0; k < F3_RANDSIZ; k++) {
+      unsigned long v = irand(&spec->rc);
+      if (t == 0 && k < 4) w[k] = (uint32_t)v;
+    }
+  uint64_t salt = f3g_opts.seed_salt;
+  key[0] = w[0] ^ (w[2] << 7 | w[2] >> 25) ^ (uint32_t)salt;
+  key[1] = w[1] ^ (w[3] << 13 | w[3] >> 19) ^ (uint32_t)(salt >> 32);
+}
+
+/* ISAAC (isaac.c:25-45 with RANDSIZL 4), to advance the caller's context */
+static void isaac_gen(randctx *ctx) {
+  unsigned long a = ctx->randa, b, x, y, *m, *mm = ctx->randmem, *m2, *r = ctx->randrsl, *mend;
+  b = (ctx->randb + (++ctx->randc)) & 0xffffffff;
+#define IND(x) (mm[((x) >> 2) & (F3_RANDSIZ - 1)])
+#define STEP(mix)                                       \
+  do {                                                  \
+    x = *m;                                             \
+    a = ((a ^ (mix)) + *(m2++)) & 0xffffffff;           \
+    *(m++) = y = (IND(x) + a + b) & 0xffffffff;         \
+    *(r++) = b = (IND(y >> F3_RANDSIZL) + x) & 0xffffffff; \
+  } while (0)
+  for (m = mm, mend = m2 = m + F3_RANDSIZ / 2; m < mend;) {
+    STEP(a << 13); STEP(a >> 6); STEP(a << 2); STEP(a >> 16);
+  }
+  for (m2 = mm; m2 < mend;) {
+    STEP(a << 13); STEP(a >> 6); STEP(a << 2); STEP(a >> 16);
+  }
+#undef STEP
+#undef IND
+  ctx->randb = b;
+  ctx->randa = a;
+}
+
+static unsigned long irand(randctx *r) {
+  if (!r->randcnt--) {
+    isaac_gen(r);
+    r->randcnt = F3_RANDSIZ - 1;
+  }
+  return r->randrsl[r->randcnt];
+}
+
+static float *upload_floats(f3g_ctx *c, float **dptr, size_t *cap, const double *src, size_t n) {
+  float *tmp = (float *)malloc(n * sizeof(float));
+  for (size_t i = 0; i < n; i++) tmp[i] = (float)src[i];
+  if (f3g_ensure((void **)dptr, cap, n * sizeof(float))) {
+    free(tmp);
+    return NULL;
+  }
+  cudaError_t e = cudaMemcpyAsync(*dptr, tmp, n * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+  cudaStreamSynchronize(c->stream);
+  free(tmp);
+  return e == cudaSuccess ? *dptr : NULL;
+}
+
+int flam3gpu_histogram_dims(flam3_frame *f, int field, int *w, int *h, int *gutter, int *de_offset,
+                            int *filter_width) {
+  f3g_clear_error();
+  flam3_genome cp;
+  memset(&cp, 0, sizeof(cp));
+  if (f3g_interpolate(f->genomes, f->ngenomes, f->time, &cp)) return 1;
+  f3g_geom g;
+  int rc = compute_geom(f, &cp, field, NULL, &g);
+  f3g_genome_free(&cp);
+  if (rc) return 1;
+  if (w) *w = g.W;
+  if (h) *h = g.H;
+  if (gutter) *gutter = g.gutter;
+  if (de_offset) *de_offset = g.de_offset;
+  if (filter_width) *filter_width = g.filter_width;
+  return 0;
+}
+
+static double now_s(void) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return t.tv_sec + 1e-9 * t.tv_nsec;
+}
+
+int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int transp, stat_struct *stats,
+                       flam3gpu_render_io *io) {
+  f3g_clear_error();
+  double t_iter = 0, t_de = 0, t_tail = 0;
+  int launches = 0;
+  double h2d = 0, d2h = 0, plotted = 0;
+  double wall0 = now_s();
+  time_t tstart = time(NULL);
+  int bits = spec->bits;
+  if (bits != 32 && bits != 33 && bits != 64) {
+    f3g_set_error("flam3: bits must be 32, 33, or 64 not %d.", bits);
+    return 1;
+  }
+  if (nchan != 3 && nchan != 4) {
+    f3g_set_error("nchan must be 3 or 4, not %d", nchan);
+    return 1;
+  }
+  f3g_ctx *c = f3g_get_ctx();
+  if (!c) {
+    f3g_set_error("no CUDA device available");
+    return 1;
+  }
+  stats->num_iters = 0;
+  stats->badvals = 0;
+  const char *ap = getenv("apo_palette");
+  int cmap_size = 256 - (ap ? atoi(ap) : 0);
+  if (cmap_size < 2 || cmap_size > 256) {
+    f3g_set_error("apo_palette gives a colour map of %d entries", cmap_size);
+    return 1;
+  }
+  flam3_genome cp;
+  memset(&cp, 0, sizeof(cp));
+  if (f3g_interpolate(spec->genomes, spec->ngenomes, spec->time, &cp)) return 1;
+  int rv = 1;
+  double *filter = NULL, *tfilter = NULL, *tdeltas = NULL, *de_w = NULL, *de_c = NULL;
+  int nbatches = cp.nbatches, ntemporal = cp.ntemporal_samples;
+  double highpow = cp.highlight_power;
+  f3g_geom g;
+  if (nbatches < 1) {
+    f3g_set_error("nbatches must be positive, not %d.", nbatches);
+    goto done;
+  }
+  if (cp.spatial_oversample < 1) {
+    f3g_set_error("oversample must be positive, not %d.", cp.spatial_oversample);
+    goto done;
+  }
+  if (ntemporal < 1) {
+    f3g_set_error("temporal samples must be positive, not %d.", ntemporal);
+    goto done;
+  }
+  if (compute_geom(spec, &cp, field, &filter, &g)) goto done;
+  if (io) {
+    io->hist_w = g.W;
+    io->hist_h = g.H;
+  }
+  double sumfilt = f3g_temporal_filter(nbatches * ntemporal, cp.temporal_filter_type, cp.temporal_filter_exp,
+                                       cp.temporal_filter_width, &tfilter, &tdeltas);
+  const long long nb = (long long)g.W * g.H;
+  const int bkind = bits == 64 ? F3G_BK_F64 : F3G_BK_F32;
+  const size_t bsz = bkind == F3G_BK_F64 ? 32 : 16;
+  const size_t csz = bkind == F3G_BK_F64 ? 8 : 4;
+  /* does the fifth (count) channel differ from alpha?  only for palettes
+   * with alpha != 1 or temporal filter weights != 1 (rect.c:778-782) */
+  int need_count = 0;
+  for (int i = 0; i < nbatches * ntemporal; i++)
+    if (tfilter[i] != 1.0) need_count = 1;
+  const int threads = f3g_opts.threads_per_block > 0 ? f3g_opts.threads_per_block : 256;
+  if (f3g_ensure(&c->d_hist, &c->hist_bytes, (size_t)nb * bsz)) goto done;
+  if (f3g_ensure(&c->d_acc, &c->acc_bytes, (size_t)nb * bsz)) goto done;
+  size_t out_bytes = (size_t)g.image_width * g.image_height * nchan * spec->bytes_per_channel;
+  if (f3g_ensure((void **)&c->d_out, &c->out_bytes, out_bytes)) goto done;
+  if (!upload_floats(c, &c->d_filter, &c->filter_bytes, filter, (size_t)g.filter_width * g.filter_width)) goto done;
+  h2d += (double)g.filter_width * g.filter_width * sizeof(float);
+  CK(cudaMemsetAsync(c->d_acc, 0, (size_t)nb * bsz, c->stream));
+  if (ensure_host_passes(c, (size_t)ntemporal)) goto done;
+  if (f3g_ensure((void **)&c->d_passes, &c->passes_bytes, (size_t)ntemporal * sizeof(F3GPass))) goto done;
+  if (f3g_ensure((void **)&c->d_prefix, &c->prefix_bytes, (size_t)(ntemporal + 1) * sizeof(long long))) goto done;
+  const int precision = f3g_opts.iter_precision == 64 ? 64 : 32;
+  double vibrancy = 0.0, gamma = 0.0, background[3] = {0, 0, 0};
+  int vib_gam_n = 0;
+  double ppux = 0, ppuy = 0, sample_density = 0;
+  const int fused_tail = (nbatches == 1) && !(io && io->accum_out);
+  int de_used_any = 0;
+
+  for (int batch = 0; batch < nbatches; batch++) {
+    double de_time = spec->time + tdeltas[batch * ntemporal];
+    int mfc = 0, mfi = 0, ks = 0;
+    free(de_w);
+    free(de_c);
+    de_w = de_c = NULL;
+    if (f3g_interpolate(spec->genomes, spec->ngenomes, de_time, &cp)) goto done;
+    if (cp.estimator < 0.0 || cp.estimator_minimum < 0.0) {
+      f3g_set_error("density estimator filter widths must be >= 0");
+      goto done;
+    }
+    if (bits <= 32 && cp.estimator > 0.0) {
+      fprintf(stderr, "warning: density estimation disabled with %d bit buffers.\n", bits);
+      cp.estimator = 0.0;
+    }
+    if (cp.estimator > 0.0) {
+      ks = f3g_de_filters(cp.estimator, cp.estimator_minimum, cp.estimator_curve, g.oversample, &mfc, &mfi, &de_w,
+                          &de_c);
+      if (ks < 0) goto done;
+    }
+    const int de_on = mfi > 0;
+    de_used_any |= de_on;
+    int use_count = de_on && need_count;
+    CK(cudaMemsetAsync(c->d_hist, 0, (size_t)nb * bsz, c->stream));
+    if (use_count) {
+      if (f3g_ensure(&c->d_count, &c->count_bytes, (size_t)nb * csz)) goto done;
+      CK(cudaMemsetAsync(c->d_count, 0, (size_t)nb * csz, c->stream));
+    }
+    /* ---- passes of this batch ---- */
+    long long total_chunks = 0, batch_samples = 0;
+    for (int ts = 0; ts < ntemporal; ts++) {
+      double color_scalar = tfilter[batch * ntemporal + ts];
+      double tst = spec->time + tdeltas[batch * ntemporal + ts];
+      F3GPass *p = &c->h_passes[ts];
+      memset(p, 0, offsetof(F3GPass, xf));
+      if (f3g_interpolate(spec->genomes, spec->ngenomes, tst, &cp)) goto done;
+      if (f3g_prepare_precalc_flags(&cp)) goto done;
+      if (f3g_build_distrib(&cp, p)) goto done;
+      for (int i = 0; i < cp.num_xforms; i++) f3g_xform_precalc(&cp, i);
+      if (f3g_pack_genome(&cp, p)) goto done;
+      for (int j = 0; j < 256; j++) {
+        for (int k = 0; k < 4; k++) p->dmap[j][k] = (float)((cp.palette[j].color[k] * F3G_WHITE) * color_scalar);
+        if (cp.palette[j].color[3] != 1.0) need_count = 1;
+      }
+      p->cmap_size = cmap_size;
+      p->palette_mode = cp.palette_mode;
+      if (set_camera(spec, &cp, field, &g, p, &sample_density, &ppux, &ppuy)) goto done;
+      double nsamples = sample_density * g.image_width * g.image_height;
+      double batch_size = nsamples / (nbatches * ntemporal);
+      stats->num_iters += batch_size;
+      p->samples = (long long)batch_size;
+      p->fuse = spec->earlyclip ? 100 : 15;
+      p->iter_mode = (cp.chaos_enable || f3g_opts.iter_mode == 0) ? 0 : 1;
+      p->buckets = c->d_hist;
+      p->count = use_count ? c->d_count : NULL;
+      p->bucket_kind = bkind;
+      consume_rc(spec, p->key);
+      batch_samples += p->samples;
+      vibrancy += cp.vibrancy;
+      gamma += cp.gamma;
+      background[0] += cp.background[0];
+      background[1] += cp.background[1];
+      background[2] += cp.background[2];
+      vib_gam_n++;
+    }
+    if (use_count == 0 && de_on && need_count) {
+      /* palette alpha != 1 found while packing: redo the batch with a count plane */
+      use_count = 1;
+      if (f3g_ensure(&c->d_count, &c->count_bytes, (size_t)nb * csz)) goto done;
+      CK(cudaMemsetAsync(c->d_count, 0, (size_t)nb * csz, c->stream));
+      for (int ts = 0; ts < ntemporal; ts++) c->h_passes[ts].count = c->d_count;
+    }
+    if (!(io && io->hist_in)) {
+      int occ = f3g_iterate_occupancy(precision, 1, threads);
+      if (occ < 1) occ = 1;
+      int blocks = f3g_opts.blocks > 0 ? f3g_opts.blocks : c->nsm * occ;
+      int S = f3g_chunk_samples(c, batch_samples, threads, blocks, spec->sub_batch_size);
+      int full = 0;
+      for (int ts = 0; ts < ntemporal; ts++) {
+        F3GPass *p = &c->h_passes[ts];
+        p->chunk_begin = total_chunks;
+        p->nchunks = (p->samples + (long long)threads * S - 1) / ((long long)threads * S);
+        total_chunks += p->nchunks;
+        c->h_prefix[ts] = p->chunk_begin;
+        full |= p->full_variations;
+      }
+      c->h_prefix[ntemporal] = total_chunks;
+      occ = f3g_iterate_occupancy(precision, full, threads);
+      if (occ < 1) occ = 1;
+      blocks = f3g_opts.blocks > 0 ? f3g_opts.blocks : c->nsm * occ;
+      CK(cudaMemcpyAsync(c->d_passes, c->h_passes, (size_t)ntemporal * sizeof(F3GPass),
+                               cudaMemcpyHostToDevice, c->stream));
+      h2d += (double)ntemporal * sizeof(F3GPass) + (double)(ntemporal + 1) * sizeof(long long);
+      CK(cudaMemcpyAsync(c->d_prefix, c->h_prefix, (size_t)(ntemporal + 1) * sizeof(long long),
+                               cudaMemcpyHostToDevice, c->stream));
+      int shuffle = f3g_opts.shuffle_every > 0 ? f3g_opts.shuffle_every : 1;
+      /* rounds: one launch, or ~10 launches with progress callbacks between */
+      int nrounds = spec->progress ? 10 : 1;
+      long long per_round = (total_chunks + nrounds - 1) / nrounds;
+      if (per_round < 1) per_round = 1;
+      for (long long lo = 0; lo < total_chunks; lo += per_round) {
+        long long hi = lo + per_round < total_chunks ? lo + per_round : total_chunks;
+        F3GCounters init;
+        memset(&init, 0, sizeof(init));
+        init.next_chunk = (unsigned long long)lo;
+        *c->h_ctr = init;
+        CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(F3GCounters), cudaMemcpyHostToDevice, c->stream));
+        h2d += sizeof(F3GCounters);
+        d2h += sizeof(F3GCounters);
+        CK(cudaEventRecord(c->ev[0], c->stream));
+        int e = f3g_launch_iterate(c->d_passes, c->d_prefix, ntemporal, hi, S, shuffle, precision, full, threads,
+                                   blocks, c->d_ctr, c->stream);
+        launches++;
+        if (e) {
+          f3g_set_error("iterate launch failed: %s", cudaGetErrorString((cudaError_t)e));
+          goto done;
+        }
+        CK(cudaEventRecord(c->ev[1], c->stream));
+        CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(F3GCounters), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        t_iter += ms;
+        stats->badvals += (double)c->h_ctr->badvals;
+        plotted += (double)c->h_ctr->plotted;
+        if (spec->progress) {
+          double pct = 100.0 * ((double)batch + (double)hi / (double)total_chunks) / nbatches;
+          int r = spec->progress(spec->progress_parameter, pct, 0, 0.0);
+          while (r == 2) {
+            struct timespec ts = {0, 100000000};
+            nanosleep(&ts, NULL);
+            r = spec->progress(spec->progress_parameter, pct, 0, 0.0);
+          }
+          if (r == 1) {
+            rv = 0;
+            goto done; /* abort: return 0 with the output as it stands (rect.c:919-922) */
+          }
+        }
+      }
+    } else {
+      /* injected histogram (R,G,B,A,count doubles per bucket) */
+      size_t n5 = (size_t)nb * 5;
+      void *hb = malloc((size_t)nb * bsz);
+      void *hc = use_count ? malloc((size_t)nb * csz) : NULL;
+      for (size_t b = 0; b < (size_t)nb; b++) {
+        const double *s = io->hist_in + 5 * b;
+        if (bkind == F3G_BK_F64) {
+          memcpy((double *)hb + 4 * b, s, 4 * sizeof(double));
+          if (hc) ((double *)hc)[b] = s[4];
+        } else {
+          for (int k = 0; k < 4; k++) ((float *)hb)[4 * b + k] = (float)s[k];
+          if (hc) ((float *)hc)[b] = (float)s[4];
+        }
+      }
+      (void)n5;
+      cudaError_t e1 = cudaMemcpy(c->d_hist, hb, (size_t)nb * bsz, cudaMemcpyHostToDevice);
+      cudaError_t e2 = hc ? cudaMemcpy(c->d_count, hc, (size_t)nb * csz, cudaMemcpyHostToDevice) : cudaSuccess;
+      free(hb);
+      free(hc);
+      if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        f3g_set_error("histogram upload failed");
+        goto done;
+      }
+    }
+    if (io && io->hist_out) {
+      void *hb = malloc((size_t)nb * bsz);
+      void *hc = use_count ? malloc((size_t)nb * csz) : NULL;
+      CK(cudaStreamSynchronize(c->stream));
+      cudaMemcpy(hb, c->d_hist, (size_t)nb * bsz, cudaMemcpyDeviceToHost);
+      if (hc) cudaMemcpy(hc, c->d_count, (size_t)nb * csz, cudaMemcpyDeviceToHost);
+      for (size_t b = 0; b < (size_t)nb; b++) {
+        double *d = io->hist_out + 5 * b;
+        for (int k = 0; k < 4; k++)
+          d[k] = bkind == F3G_BK_F64 ? ((double *)hb)[4 * b + k] : (double)((float *)hb)[4 * b + k];
+        d[4] = hc ? (bkind == F3G_BK_F64 ? ((double *)hc)[b] : (double)((float *)hc)[b]) : d[3];
+      }
+      free(hb);
+      free(hc);
+    }
+    /* ---- k1/k2 and density estimation (rect.c:933-1050) ---- */
+    double k1 = (cp.contrast * cp.brightness * 255.0 * 268.0 * (1.0 / nbatches)) / 256;
+    double area = g.image_width * g.image_height / (ppux * ppuy);
+    double k2 = (g.oversample * g.oversample * nbatches) / (cp.contrast * area * F3G_WHITE * sample_density * sumfilt);
+    if (fused_tail && !de_on) {
+      /* the fused tail below reads the histogram directly */
+      c->timings[1] = 0;
+      goto tail_fused;
+    }
+    CK(cudaEventRecord(c->ev[2], c->stream));
+    if (de_on) {
+      int R = (int)ceil(de_w[0]) - 1;
+      if (R > f3g_de_max_reach()) {
+        f3g_set_error("density estimation radius %d exceeds this build's limit %d", R, f3g_de_max_reach());
+        goto done;
+      }
+      int nk = mfi + 1;
+      if (!upload_floats(c, &c->d_de_w, &c->de_w_bytes, de_w, (size_t)nk)) goto done;
+      if (!upload_floats(c, &c->d_de_c, &c->de_c_bytes, de_c, (size_t)nk * ks)) goto done;
+      h2d += (double)nk * (ks + 1) * sizeof(float);
+      int e = f3g_launch_de(c->d_hist, bkind, use_count ? c->d_count : NULL, g.W, g.H, g.oversample, k1, k2,
+                            cp.estimator_curve, mfc, mfi, ks, c->d_de_w, c->d_de_c, R, c->d_acc, bkind, c->stream);
+      launches++;
+      if (e) {
+        f3g_set_error("density estimation launch failed: %s", cudaGetErrorString((cudaError_t)e));
+        goto done;
+      }
+    } else {
+      int e = f3g_launch_logscale(c->d_hist, bkind, nb, k1, k2, c->d_acc, bkind, c->stream);
+      launches++;
+      if (e) {
+        f3g_set_error("log scaling launch failed: %s", cudaGetErrorString((cudaError_t)e));
+        goto done;
+      }
+    }
+    CK(cudaEventRecord(c->ev[3], c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+      t_de += ms;
+    }
+    if (spec->progress) {
+      int r = spec->progress(spec->progress_parameter, 100.0 * (batch + 1) / nbatches, 1, 0.0);
+      if (r == 1) {
+        rv = 0;
+        goto done;
+      }
+    }
+  }
+
+  if (io && io->accum_out) {
+    size_t n4 = (size_t)nb * 4;
+    void *ha = malloc((size_t)nb * bsz);
+    CK(cudaStreamSynchronize(c->stream));
+    cudaMemcpy(ha, c->d_acc, (size_t)nb * bsz, cudaMemcpyDeviceToHost);
+    for (size_t k = 0; k < n4; k++)
+      io->accum_out[k] = bkind == F3G_BK_F64 ? ((double *)ha)[k] : (double)((float *)ha)[k];
+    free(ha);
+  }
+
+tail_fused:;
+  {
+    /* ---- filter + tonemap + pack (rect.c:1067-1247) ---- */
+    F3GTonemap tp;
+    double gm = 1.0 / (gamma / vib_gam_n);
+    tp.g = (float)gm;
+    tp.linrange = (float)cp.gam_lin_thresh;
+    tp.funcval = (float)pow(cp.gam_lin_thresh, gm);
+    tp.vibrancy = (float)(vibrancy / vib_gam_n);
+    tp.highpow = (float)highpow;
+    for (int k = 0; k < 3; k++) tp.background[k] = (float)(background[k] / (vib_gam_n / 256.0));
+    tp.nchan = nchan;
+    tp.transp = transp;
+    tp.bpc = spec->bytes_per_channel;
+    CK(cudaEventRecord(c->ev[4], c->stream));
+    int e;
+    if (fused_tail && !de_used_any) {
+      double k1 = (cp.contrast * cp.brightness * 255.0 * 268.0 * 1.0) / 256;
+      double area = g.image_width * g.image_height / (ppux * ppuy);
+      double k2 = (g.oversample * g.oversample * 1) / (cp.contrast * area * F3G_WHITE * sample_density * sumfilt);
+      e = f3g_launch_fused_log_filter(c->d_hist, bkind, g.W, g.H, k1, k2, g.de_offset, g.oversample, c->d_filter,
+                                      g.filter_width, g.image_width, g.image_height, c->d_out, spec->earlyclip, &tp,
+                                      c->stream);
+      launches++;
+    } else {
+      e = 0;
+      if (spec->earlyclip) {
+        e = f3g_launch_earlyclip(c->d_acc, bkind, nb, &tp, c->stream);
+        launches++;
+      }
+      if (!e) {
+        e = f3g_launch_filter_tonemap(c->d_acc, bkind, g.W, g.de_offset, g.oversample, c->d_filter, g.filter_width,
+                                      g.image_width, g.image_height, c->d_out, spec->earlyclip, &tp, c->stream);
+        launches++;
+      }
+    }
+    if (e) {
+      f3g_set_error("filter/tonemap launch failed: %s", cudaGetErrorString((cudaError_t)e));
+      goto done;
+    }
+    CK(cudaEventRecord(c->ev[5], c->stream));
+    size_t row = (size_t)g.image_width * nchan * spec->bytes_per_channel;
+    unsigned char *dst = (unsigned char *)out;
+    if (field == flam3_field_odd) dst += row;
+    size_t dpitch = (size_t)g.out_width * nchan * spec->bytes_per_channel;
+    CK(cudaMemcpy2DAsync(dst, dpitch, c->d_out, row, row, (size_t)g.image_height, cudaMemcpyDeviceToHost,
+                               c->stream));
+    d2h += (double)row * g.image_height;
+    CK(cudaStreamSynchronize(c->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]);
+    t_tail = ms;
+  }
+  rv = 0;
+
+done:
+  c->timings[0] = t_iter;
+  c->timings[1] = t_de;
+  c->timings[2] = t_tail;
+  c->timings[3] = 1e3 * (now_s() - wall0);
+  c->timings[4] = launches;
+  c->timings[5] = h2d;
+  c->timings[6] = d2h;
+  c->timings[7] = plotted;
+  free(filter);
+  free(tfilter);
+  free(tdeltas);
+  free(de_w);
+  free(de_c);
+  f3g_genome_free(&cp);
+  stats->render_seconds = (int)(time(NULL) - tstart);
+  if (rv) fprintf(stderr, "flam3gpu: %s\n", flam3gpu_last_error());
+  return rv;
+}
+
+int flam3gpu_render(flam3_frame *f, void *out, int field, int nchan, int transp, stat_struct *stats) {
+  return flam3gpu_render_ex(f, out, field, nchan, transp, stats, NULL);
+}
+
+double flam3gpu_render_memory_required(flam3_frame *f) {
+  flam3_genome *cp = &f->genomes[0];
+  int bsz = f->bits == 64 ? 32 : 16;
+  double nb = (double)cp->spatial_oversample * cp->spatial_oversample * (double)cp->width * cp->height;
+  return nb * bsz * 2.0 + (double)cp->width * cp->height * 4 * 2;
+}
+
+int flam3gpu_last_timings(double t[8]) {
+  f3g_ctx *c = f3g_get_ctx();
+  if (!c) return 1;
+  for (int i = 0; i < 8; i++) t[i] = c->timings[i];
+  return 0;
+}
+
+/* GPU bucket accumulation of a given point stream (rect.c:411-516) into a
+ * FP64 histogram of the render geometry; the result is added to `hist`
+ * (5 doubles per bucket). */
+int f3g_accumulate_impl(flam3_frame *f, int field, const double *points, long n, double *hist, int *hist_w,
+                        int *hist_h) {
+  f3g_ctx *c = f3g_get_ctx();
+  if (!c) {
+    f3g_set_error("no CUDA device available");
+    return 1;
+  }
+  flam3_genome cp;
+  memset(&cp, 0, sizeof(cp));
+  int rv = 1;
+  double *d_pts = NULL, *h4 = NULL, *hc = NULL;
+  void *d_b = NULL, *d_c = NULL;
+  size_t cap_b = 0, cap_c = 0;
+  if (f3g_interpolate(f->genomes, f->ngenomes, f->time, &cp)) return 1;
+  f3g_geom g;
+  if (compute_geom(f, &cp, field, NULL, &g)) goto done;
+  *hist_w = g.W;
+  *hist_h = g.H;
+  if (!hist) {
+    rv = 0;
+    goto done;
+  }
+  if (ensure_host_pass_one(c)) goto done;
+  F3GPass *p = c->h_passes;
+  memset(p, 0, sizeof(*p));
+  const char *ap = getenv("apo_palette");
+  p->cmap_size = 256 - (ap ? atoi(ap) : 0);
+  if (p->cmap_size < 2 || p->cmap_size > 256) {
+    f3g_set_error("apo_palette gives a colour map of %d entries", p->cmap_size);
+    goto done;
+  }
+  p->palette_mode = cp.palette_mode;
+  for (int j = 0; j < 256; j++)
+    for (int k = 0; k < 4; k++) p->dmap[j][k] = (float)(cp.palette[j].color[k] * F3G_WHITE);
+  double sd, px, py;
+  if (set_camera(f, &cp, field, &g, p, &sd, &px, &py)) goto done;
+  long long nb = (long long)g.W * g.H;
+  if (f3g_ensure(&d_b, &cap_b, (size_t)nb * 32) || f3g_ensure(&d_c, &cap_c, (size_t)nb * 8)) goto done;
+  CK(cudaMemset(d_b, 0, (size_t)nb * 32));
+  CK(cudaMemset(d_c, 0, (size_t)nb * 8));
+  p->buckets = d_b;
+  p->count = d_c;
+  p->bucket_kind = F3G_BK_F64;
+  if (f3g_ensure((void **)&c->d_passes, &c->passes_bytes, sizeof(F3GPass))) goto done;
+  CK(cudaMemcpy(c->d_passes, p, sizeof(F3GPass), cudaMemcpyHostToDevice));
+  if (n > 0) {
+    CK(cudaMalloc((void **)&d_pts, (size_t)n * 4 * sizeof(double)));
+    CK(cudaMemcpy(d_pts, points, (size_t)n * 4 * sizeof(double), cudaMemcpyHostToDevice));
+    if (f3g_launch_accumulate(c->d_passes, d_pts, n, c->stream)) {
+      f3g_set_error("accumulate launch failed");
+      goto done;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  h4 = (double *)malloc((size_t)nb * 32);
+  hc = (double *)malloc((size_t)nb * 8);
+  CK(cudaMemcpy(h4, d_b, (size_t)nb * 32, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hc, d_c, (size_t)nb * 8, cudaMemcpyDeviceToHost));
+  for (long long b = 0; b < nb; b++) {
+    for (int k = 0; k < 4; k++) hist[5 * b + k] += h4[4 * b + k];
+    hist[5 * b + 4] += hc[b];
+  }
+  rv = 0;
+done:
+  cudaFree(d_pts);
+  cudaFree(d_b);
+  cudaFree(d_c);
+  free(h4);
+  free(hc);
+  f3g_genome_free(&cp);
+  return rv;
+}

@@ -1,0 +1,187 @@
+"""Python view of libflam3gpu's C ABI (include/flam3_gpu.h).
+
+`render(frame, ...)` is flam3_render (flam3.h:623) on the GPU: same frame,
+same output layout, same stats.  The other functions expose the kernel-level
+entry points used for parity work.  Every call goes through the native
+library; if it is not built, `load()` raises -- there is no fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_LIB = None
+_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libflam3gpu.so")
+
+
+class Flam3GpuError(RuntimeError):
+    pass
+
+
+class RenderIO(C.Structure):
+    _fields_ = [("hist_in", C.POINTER(C.c_double)), ("hist_out", C.POINTER(C.c_double)),
+                ("accum_out", C.POINTER(C.c_double)), ("hist_w", C.c_int), ("hist_h", C.c_int),
+                ("reserved", C.c_int * 6)]
+
+
+class Options(C.Structure):
+    _fields_ = [("iter_mode", C.c_int), ("iter_precision", C.c_int), ("shuffle_every", C.c_int),
+                ("threads_per_block", C.c_int), ("blocks", C.c_int), ("chain_samples", C.c_int),
+                ("seed_salt", C.c_uint64), ("reserved", C.c_int * 8)]
+
+
+def load():
+    """Load libflam3gpu.so (built by flam3_gb300._build / __graft_entry__.build)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(_LIB_PATH):
+        raise Flam3GpuError(f"{_LIB_PATH} is not built; run `python -m flam3_gb300._build`")
+    lib = C.CDLL(_LIB_PATH)
+    F = C.POINTER(abi.flam3_frame)
+    G = C.POINTER(abi.flam3_genome)
+    S = C.POINTER(abi.stat_struct)
+    dp = C.POINTER(C.c_double)
+    lib.flam3gpu_render.argtypes = [F, C.c_void_p, C.c_int, C.c_int, C.c_int, S]
+    lib.flam3gpu_render_ex.argtypes = [F, C.c_void_p, C.c_int, C.c_int, C.c_int, S, C.POINTER(RenderIO)]
+    lib.flam3gpu_render_memory_required.argtypes = [F]
+    lib.flam3gpu_render_memory_required.restype = C.c_double
+    lib.flam3gpu_last_error.restype = C.c_char_p
+    lib.flam3gpu_version.restype = C.c_char_p
+    lib.flam3gpu_set_options.argtypes = [C.POINTER(Options)]
+    lib.flam3gpu_get_options.argtypes = [C.POINTER(Options)]
+    lib.flam3gpu_default_options.argtypes = [C.POINTER(Options)]
+    lib.flam3gpu_last_timings.argtypes = [dp]
+    lib.flam3gpu_histogram_dims.argtypes = [F, C.c_int] + [C.POINTER(C.c_int)] * 5
+    lib.flam3gpu_apply_xform.argtypes = [G, C.c_int, C.c_int, dp, C.POINTER(C.c_uint32), C.c_int, dp,
+                                         C.POINTER(C.c_int), C.c_int]
+    lib.flam3gpu_accumulate_points.argtypes = [F, C.c_int, dp, C.c_long, dp, C.POINTER(C.c_int),
+                                               C.POINTER(C.c_int)]
+    lib.flam3gpu_iterate_chains.argtypes = [G, C.c_int, C.c_int, C.c_int, dp, C.c_uint64, dp,
+                                            C.POINTER(C.c_long), C.c_int]
+    _LIB = lib
+    return lib
+
+
+def _err(lib, what):
+    raise Flam3GpuError(f"{what} failed: {lib.flam3gpu_last_error().decode()}")
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def version():
+    return load().flam3gpu_version().decode()
+
+
+def histogram_dims(frame, field=0):
+    lib = load()
+    v = [C.c_int() for _ in range(5)]
+    if lib.flam3gpu_histogram_dims(C.byref(frame.f), field, *[C.byref(x) for x in v]):
+        _err(lib, "histogram_dims")
+    w, h, gutter, de_offset, fw = (x.value for x in v)
+    return {"w": w, "h": h, "gutter": gutter, "de_offset": de_offset, "filter_width": fw}
+
+
+def render(frame, field=0, nchan=3, transp=0, out=None, hist_in=None, want_hist=False, want_accum=False):
+    """flam3_render on the GPU.  Returns (image, stats[, extras])."""
+    lib = load()
+    if out is None:
+        out = frame.out_buffer(nchan)
+    st = abi.stat_struct()
+    extras = {}
+    if hist_in is None and not want_hist and not want_accum:
+        if lib.flam3gpu_render(C.byref(frame.f), out.ctypes.data, field, nchan, transp, C.byref(st)):
+            _err(lib, "flam3gpu_render")
+        return out, st
+    d = histogram_dims(frame, field)
+    io = RenderIO()
+    if hist_in is not None:
+        hist_in = np.ascontiguousarray(hist_in, dtype=np.float64)
+        if hist_in.size != d["w"] * d["h"] * 5:
+            raise ValueError("hist_in has the wrong size")
+        io.hist_in = _dptr(hist_in)
+    if want_hist:
+        extras["hist"] = np.zeros((d["h"], d["w"], 5))
+        io.hist_out = _dptr(extras["hist"])
+    if want_accum:
+        extras["accum"] = np.zeros((d["h"], d["w"], 4))
+        io.accum_out = _dptr(extras["accum"])
+    if lib.flam3gpu_render_ex(C.byref(frame.f), out.ctypes.data, field, nchan, transp, C.byref(st), C.byref(io)):
+        _err(lib, "flam3gpu_render_ex")
+    return out, st, extras
+
+
+def memory_required(frame):
+    return load().flam3gpu_render_memory_required(C.byref(frame.f))
+
+
+def last_timings():
+    """Measurements of the last render on this thread: kernel times (ms,
+    CUDA events), wall time, kernel launches, host<->device bytes, samples
+    plotted."""
+    t = (C.c_double * 8)()
+    load().flam3gpu_last_timings(t)
+    return {"iterate_ms": t[0], "de_ms": t[1], "tail_ms": t[2], "wall_ms": t[3], "launches": int(t[4]),
+            "h2d_bytes": int(t[5]), "d2h_bytes": int(t[6]), "plotted": int(t[7])}
+
+
+def get_options():
+    o = Options()
+    load().flam3gpu_get_options(C.byref(o))
+    return o
+
+
+def set_options(**kw):
+    lib = load()
+    o = get_options()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    if lib.flam3gpu_set_options(C.byref(o)):
+        _err(lib, "set_options")
+
+
+def reset_options():
+    lib = load()
+    o = Options()
+    lib.flam3gpu_default_options(C.byref(o))
+    lib.flam3gpu_set_options(C.byref(o))
+
+
+def apply_xform(genome, fn, points, words, precision=64):
+    lib = load()
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 4)
+    n = pts.shape[0]
+    w = np.ascontiguousarray(words, dtype=np.uint32).reshape(n, -1)
+    q = np.zeros((n, 4))
+    bad = np.zeros(n, dtype=np.int32)
+    if lib.flam3gpu_apply_xform(C.byref(genome.g), fn, n, _dptr(pts), w.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                w.shape[1], _dptr(q), bad.ctypes.data_as(C.POINTER(C.c_int)), precision):
+        _err(lib, "apply_xform")
+    return q, bad
+
+
+def iterate_chains(genome, starts, n, fuse, seed, precision=64):
+    lib = load()
+    st = np.ascontiguousarray(starts, dtype=np.float64).reshape(-1, 4)
+    out = np.zeros((st.shape[0], n, 4))
+    bad = C.c_long()
+    if lib.flam3gpu_iterate_chains(C.byref(genome.g), st.shape[0], n, fuse, _dptr(st), seed, _dptr(out),
+                                   C.byref(bad), precision):
+        _err(lib, "iterate_chains")
+    return out, bad.value
+
+
+def accumulate_points(frame, points, field=0):
+    lib = load()
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 4)
+    w, h = C.c_int(), C.c_int()
+    lib.flam3gpu_accumulate_points(C.byref(frame.f), field, _dptr(pts), 0, None, C.byref(w), C.byref(h))
+    hist = np.zeros((h.value, w.value, 5))
+    if lib.flam3gpu_accumulate_points(C.byref(frame.f), field, _dptr(pts), pts.shape[0], _dptr(hist), C.byref(w),
+                                      C.byref(h)):
+        _err(lib, "accumulate_points")
+    return hist

@@ -245,11 +245,13 @@ void flam3gpu_default_options(flam3gpu_options *o);
 int flam3gpu_set_options(const flam3gpu_options *o);
 void flam3gpu_get_options(flam3gpu_options *o);
 
-/* Device-side timing of the last flam3gpu_render call on this thread, in
- * milliseconds measured with CUDA events: [0] iterate+accumulate kernels,
- * [1] density estimation / log scaling, [2] filter+tonemap+pack, [3] whole
- * call wall time, [4] number of kernel launches. */
-int flam3gpu_last_timings(double t[5]);
+/* Measurements of the last flam3gpu_render call on this thread (no
+ * counterpart in the reference): [0] iterate+accumulate kernel time, [1]
+ * density estimation / log scaling, [2] filter+tonemap+pack (ms, CUDA events
+ * on the library's stream), [3] wall time of the whole call (ms), [4] kernel
+ * launches, [5] host-to-device bytes, [6] device-to-host bytes, [7] samples
+ * plotted by the iterate kernels. */
+int flam3gpu_last_timings(double t[8]);
 
 #ifdef __cplusplus
 }

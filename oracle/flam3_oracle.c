@@ -1275,4 +1275,48 @@ static int iterate(flam3_genome *cp, int n, int fuse, double *samples, unsigned 
   return badvals;
 }
 
+
 #include "flam3_oracle_render.inc"
+
+/* Chains of flam3_iterate (flam3.c:232-299) driven by the CUDA path's
+ * Philox stream: chain c draws from key (seed lo, seed hi), counter
+ * (c, block, 0, 0xC4A1) -- the same words the GPU's recorded-chain probe
+ * consumes -- so both sides pick the same xforms and random parameters. */
+int f3o_iterate_chains(flam3_genome *src, int nchains, int n, int fuse, const double *starts, uint64_t seed,
+                       double *samples, long *badvals);
+
+int f3o_iterate_chains(flam3_genome *src, int nchains, int n, int fuse, const double *starts, uint64_t seed,
+                       double *samples, long *badvals) {
+  flam3_genome cp;
+  memset(&cp, 0, sizeof(cp));
+  genome_copy(&cp, src);
+  long bad = 0;
+  int rc = 1;
+  double *buf = (double *)malloc(sizeof(double) * 4 * (size_t)(n > 0 ? n : 1));
+  unsigned short *xd = NULL;
+  if (f3o_prepare_precalc_flags(&cp)) goto out;
+  xd = f3o_create_xform_distrib(&cp);
+  if (!xd) goto out;
+  for (int c = 0; c < nchains; c++) {
+    f3o_rng r;
+    memset(&r, 0, sizeof(r));
+    r.kind = 2;
+    r.key[0] = (uint32_t)seed;
+    r.key[1] = (uint32_t)(seed >> 32);
+    r.ctr[0] = (uint32_t)c;
+    r.ctr[1] = 0;
+    r.ctr[2] = 0;
+    r.ctr[3] = 0xC4A1u;
+    r.bufpos = 4;
+    memcpy(buf, starts + 4 * (size_t)c, 4 * sizeof(double));
+    bad += iterate(&cp, n, fuse, buf, xd, &r);
+    memcpy(samples + (size_t)c * n * 4, buf, sizeof(double) * 4 * (size_t)n);
+  }
+  rc = 0;
+out:
+  if (badvals) *badvals = bad;
+  free(buf);
+  free(xd);
+  genome_free(&cp);
+  return rc;
+}

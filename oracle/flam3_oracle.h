@@ -84,6 +84,10 @@ int f3o_render_ex(flam3_frame *f, void *out, int field, int nchan, int transp,
 int f3o_accumulate_points(flam3_frame *f, int field, const double *points, long n,
                           double *hist, int *hist_w, int *hist_h);
 
+/* Chains replaying the CUDA path's Philox stream (see flam3_oracle.c). */
+int f3o_iterate_chains(flam3_genome *cp, int nchains, int n, int fuse, const double *starts, uint64_t seed,
+                       double *samples, long *badvals);
+
 /* Counter-based stream used by the CUDA path (Philox4x32-10), exposed so the
  * oracle can replay the GPU's random words. */
 void f3o_philox4x32(uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

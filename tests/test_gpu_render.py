@@ -1,0 +1,118 @@
+"""Whole renders through flam3gpu_render (the drop-in) against the oracle.
+
+The GPU draws its random numbers from a counter-based stream instead of
+ISAAC, so images are compared statistically: per-channel mean absolute error
+against an oracle render at 16x the quality, which must fall as
+1/sqrt(quality); the warp-coherent mode is checked against the per-thread
+mode the same way.  Also: stats and the caller's ISAAC context advance as in
+the reference, error returns, progress-callback abort."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from flam3_gb300 import abi, genome as gm, render
+import _oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def cfg0(seed=0, w=256, h=192, q=50.0, bits=33, est=0.0):
+    G = gm.config0_genome(seed)
+    gm.resize(G, w, h)
+    G.g.sample_density = q
+    G.g.estimator = est
+    return G
+
+
+def mae(a, b):
+    return float(np.mean(np.abs(a.astype(np.float64) - b.astype(np.float64))))
+
+
+@pytest.fixture(scope="module")
+def hq_reference():
+    """Oracle render at 16x quality (and 8 worker threads)."""
+    G = cfg0(q=50.0 * 16)
+    F = gm.Frame(G, bits=64, nthreads=8, seed="hq")
+    out, st, _ = _oracle.oracle_render(F)
+    return out
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_render_matches_hq_reference_and_converges(gpulib, hq_reference, mode):
+    render.set_options(iter_mode=mode)
+    try:
+        errs = []
+        for q in (12.5, 50.0, 200.0):
+            F = gm.Frame(cfg0(q=q), bits=33, seed="gpu-%g" % q)
+            out, st = render.render(F)
+            errs.append(mae(out, hq_reference))
+        # error falls roughly as 1/sqrt(quality): 4x quality -> about half
+        assert errs[1] < 0.8 * errs[0] and errs[2] < 0.8 * errs[1], errs
+        assert errs[2] < 2.0, errs
+    finally:
+        render.reset_options()
+
+
+def test_gpu_error_comparable_to_oracle_error(gpulib, hq_reference):
+    F = gm.Frame(cfg0(q=50.0), bits=33, seed="o")
+    o, _, _ = _oracle.oracle_render(F)
+    F = gm.Frame(cfg0(q=50.0), bits=33, seed="g")
+    g, _ = render.render(F)
+    e_o, e_g = mae(o, hq_reference), mae(g, hq_reference)
+    assert e_g < 1.5 * e_o + 0.1, (e_g, e_o)
+
+
+def test_stats_and_isaac_consumption_match_reference(gpulib):
+    Fo = gm.Frame(cfg0(q=20.0), bits=33, nthreads=3, seed="rc")
+    _, so, _ = _oracle.oracle_render(Fo)
+    Fg = gm.Frame(cfg0(q=20.0), bits=33, nthreads=3, seed="rc")
+    _, sg = render.render(Fg)
+    assert sg.num_iters == so.num_iters
+    assert [Fg.f.rc.randrsl[i] for i in range(16)] == [Fo.f.rc.randrsl[i] for i in range(16)]
+    assert Fg.f.rc.randcnt == Fo.f.rc.randcnt
+
+
+def test_bad_bits_and_bad_oversample_return_1(gpulib):
+    F = gm.Frame(cfg0(q=5.0), bits=48)
+    out = F.out_buffer(3)
+    st = abi.stat_struct()
+    assert gpulib.flam3gpu_render(C.byref(F.f), out.ctypes.data, 0, 3, 0, C.byref(st)) == 1
+    G = cfg0(q=5.0)
+    G.g.spatial_oversample = 0
+    F = gm.Frame(G, bits=33)
+    assert gpulib.flam3gpu_render(C.byref(F.f), out.ctypes.data, 0, 3, 0, C.byref(st)) == 1
+    G = cfg0(q=5.0)
+    G.xform(0).density = -1.0
+    F = gm.Frame(G, bits=33)
+    assert gpulib.flam3gpu_render(C.byref(F.f), out.ctypes.data, 0, 3, 0, C.byref(st)) == 1
+
+
+def test_progress_abort_returns_0(gpulib):
+    calls = []
+
+    @abi.PROGRESS_FN
+    def prog(param, pct, stage, eta):
+        calls.append(pct)
+        return 1
+
+    F = gm.Frame(cfg0(q=20.0), bits=33)
+    F.f.progress = prog
+    out = F.out_buffer(3)
+    st = abi.stat_struct()
+    assert gpulib.flam3gpu_render(C.byref(F.f), out.ctypes.data, 0, 3, 0, C.byref(st)) == 0
+    assert len(calls) == 1
+
+
+def test_de_render_close_to_oracle(gpulib):
+    Fo = gm.Frame(cfg0(q=400.0, est=4.0, w=160, h=120), bits=33, nthreads=8, seed="de")
+    o, _, _ = _oracle.oracle_render(Fo)
+    Fg = gm.Frame(cfg0(q=400.0, est=4.0, w=160, h=120), bits=33, seed="de-g")
+    g, _ = render.render(Fg)
+    assert mae(o, g) < 2.5
+
+
+def test_bits64_render_close_to_bits33(gpulib):
+    a, _ = render.render(gm.Frame(cfg0(q=100.0), bits=33, seed="x"))
+    b, _ = render.render(gm.Frame(cfg0(q=100.0), bits=64, seed="x"))
+    assert mae(a, b) < 0.5

@@ -1,0 +1,55 @@
+"""libflam3gpu.so loads without a GPU and exports every function that
+include/*.h declares; option validation needs no device."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in ("flam3_gpu.h", "flam3_gpu_kernels.h"):
+        txt = open(os.path.join(ROOT, "include", h)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"\b(flam3gpu_\w+)\s*\(", txt):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_function():
+    from flam3_gb300 import _build, render
+
+    if not os.path.exists(render._LIB_PATH):
+        _build.build()
+    syms = subprocess.run(["nm", "-D", "--defined-only", render._LIB_PATH], capture_output=True, text=True,
+                          check=True).stdout
+    exported = {line.split()[-1] for line in syms.splitlines() if " T " in line}
+    names = declared_functions()
+    assert len(names) >= 13
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    lib = render.load()
+    for n in names:
+        assert hasattr(lib, n)
+
+
+def test_options_validation_without_gpu():
+    from flam3_gb300 import render
+
+    lib = render.load()
+    o = render.Options()
+    lib.flam3gpu_default_options(C.byref(o))
+    assert o.iter_mode == 1 and o.iter_precision == 32 and o.threads_per_block == 256
+    bad = render.Options.from_buffer_copy(o)
+    bad.iter_precision = 16
+    assert lib.flam3gpu_set_options(C.byref(bad)) != 0
+    assert b"iter_precision" in lib.flam3gpu_last_error()
+    bad = render.Options.from_buffer_copy(o)
+    bad.threads_per_block = 100
+    assert lib.flam3gpu_set_options(C.byref(bad)) != 0
+    assert lib.flam3gpu_set_options(C.byref(o)) == 0
+    assert render.version().startswith("flam3-gb300")
