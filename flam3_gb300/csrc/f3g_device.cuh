@@ -42,25 +42,30 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
 
 /* A stream of 32-bit words: counter (c0, block, c2, c3) under key k;
  * each refill bumps the block word and yields four words in order. */
+/* One Philox block, kept out of line (one copy of the ten rounds instead of
+ * one per draw site); arguments and result stay in registers. */
+static __device__ __noinline__ uint4 philox_block(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                           uint32_t k1) {
+  uint32_t c[4] = {c0, c1, c2, c3};
+  philox4x32_10(c, k0, k1);
+  return make_uint4(c[0], c[1], c[2], c[3]);
+}
+
 struct Rng {
   uint32_t k0, k1, c0, blk, c2, c3;
-  uint32_t buf[4];
+  uint32_t b0, b1, b2, b3;
   int pos;
   __device__ __forceinline__ void init(uint32_t key0, uint32_t key1, uint32_t ctr0, uint32_t ctr2, uint32_t ctr3) {
     k0 = key0; k1 = key1; c0 = ctr0; blk = 0; c2 = ctr2; c3 = ctr3; pos = 4;
   }
-  /* kept out of line: one copy of the 10 rounds instead of one per draw site */
-  __device__ __noinline__ void refill() {
-    uint32_t c[4] = {c0, blk, c2, c3};
-    philox4x32_10(c, k0, k1);
-    buf[0] = c[0]; buf[1] = c[1]; buf[2] = c[2]; buf[3] = c[3];
-    blk++;
-    pos = 0;
-  }
   __device__ __forceinline__ uint32_t word() {
-    if (pos == 4) refill();
-    /* dynamic index into a 4-entry register array compiles to selects */
-    uint32_t w = (pos == 0) ? buf[0] : (pos == 1) ? buf[1] : (pos == 2) ? buf[2] : buf[3];
+    if (pos == 4) {
+      uint4 r = philox_block(c0, blk, c2, c3, k0, k1);
+      b0 = r.x; b1 = r.y; b2 = r.z; b3 = r.w;
+      blk++;
+      pos = 0;
+    }
+    uint32_t w = (pos == 0) ? b0 : (pos == 1) ? b1 : (pos == 2) ? b2 : b3;
     pos++;
     return w;
   }
@@ -152,8 +157,8 @@ template <typename R> struct Helper {
 #define P(name) x.prm[PRM_##name]
 
 /* variations 0-19 (the set the common genomes use) */
-template <typename R, class G>
-__device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R> &x, G &rng) {
+template <typename R>
+__device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R> &x, uint32_t rword) {
   switch (v) {
     case 0: f.p0 += w * f.tx; f.p1 += w * f.ty; break;
     case 1: f.p0 += w * m_sin(f.tx); f.p1 += w * m_sin(f.ty); break;
@@ -196,7 +201,7 @@ __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R>
     } break;
     case 13: {
       R a = (R)0.5 * f.atan_xy, sa, ca;
-      if (rng.word() & 1u) a += PI_R;
+      if (rword & 1u) a += PI_R;
       R r = w * m_sqrt(f.sqrtv); m_sincos(a, &sa, &ca);
       f.p0 += r * ca; f.p1 += r * sa;
     } break;
@@ -230,8 +235,35 @@ __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R>
 }
 
 /* variations 20-98 */
-template <typename R, class G>
-__device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R> &x, G &rng) {
+/* Random words each of these variations draws, in order (variations.c). */
+__device__ __forceinline__ int ext_draws(int v) {
+  switch (v) {
+    case 35: return 5;
+    case 36: return 4;
+    case 37: return 3;
+    case 31: case 34: case 43: case 53: return 2;
+    case 32: case 33: case 41: case 44: case 45: case 47: case 50: case 51: case 52: case 56: case 59: case 78:
+      return 1;
+    default: return 0;
+  }
+}
+
+/* Kept out of line and free of references: inputs by value (the random words
+ * already drawn, in the order the variation consumes them), result (p0, p1)
+ * returned, so the call stays in registers. */
+template <typename R> struct Vec2;
+template <> struct Vec2<float> { typedef float2 T; };
+template <> struct Vec2<double> { typedef double2 T; };
+
+template <typename R>
+__device__ __noinline__ typename Vec2<R>::T var_extended_impl(int v, R w, R tx, R ty, R sumsq, R sqrtv, R atan_xy, R sina,
+                                                             R cosa, R atan_yx, R p0, R p1,
+                                                             const XfS<R> *__restrict__ xp, uint32_t w0, uint32_t w1,
+                                                             uint32_t w2, uint32_t w3, uint32_t w4) {
+  Helper<R> f;
+  f.tx = tx; f.ty = ty; f.sumsq = sumsq; f.sqrtv = sqrtv; f.atan_xy = atan_xy; f.sina = sina; f.cosa = cosa;
+  f.atan_yx = atan_yx; f.p0 = p0; f.p1 = p1;
+  const XfS<R> &x = *xp;
   switch (v) {
     case 20: {
       R a = f.tx * PI_R, sa, ca; m_sincos(a, &sa, &ca);
@@ -281,18 +313,18 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
       f.p0 += w * P(perspective_dist) * f.tx * t; f.p1 += w * P(persp_vfcos) * f.ty * t;
     } break;
     case 31: {
-      R tmpr = u01<R>(rng.word()) * (R)2 * PI_R, sinr, cosr; m_sincos(tmpr, &sinr, &cosr);
-      R r = w * u01<R>(rng.word());
+      R tmpr = u01<R>(w0) * (R)2 * PI_R, sinr, cosr; m_sincos(tmpr, &sinr, &cosr);
+      R r = w * u01<R>(w1);
       f.p0 += f.tx * r * cosr; f.p1 += f.ty * r * sinr;
     } break;
     case 32: {
-      int t_rnd = (int)m_trunc(P(julian_rN) * u01<R>(rng.word()));
+      int t_rnd = (int)m_trunc(P(julian_rN) * u01<R>(w0));
       R tmpr = (f.atan_yx + (R)2 * PI_R * (R)t_rnd) / P(julian_power);
       R r = w * m_pow(f.sumsq, P(julian_cn)), sina, cosa; m_sincos(tmpr, &sina, &cosa);
       f.p0 += r * cosa; f.p1 += r * sina;
     } break;
     case 33: {
-      int t_rnd = (int)m_trunc(P(juliascope_rN) * u01<R>(rng.word()));
+      int t_rnd = (int)m_trunc(P(juliascope_rN) * u01<R>(w0));
       R tmpr, sina, cosa;
       if ((t_rnd & 1) == 0) tmpr = ((R)2 * PI_R * (R)t_rnd + f.atan_yx) / P(juliascope_power);
       else tmpr = ((R)2 * PI_R * (R)t_rnd - f.atan_yx) / P(juliascope_power);
@@ -301,18 +333,18 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
       f.p0 += r * cosa; f.p1 += r * sina;
     } break;
     case 34: {
-      R tmpr = u01<R>(rng.word()) * (R)2 * PI_R, sinr, cosr; m_sincos(tmpr, &sinr, &cosr);
-      R r = w * u01<R>(rng.word());
+      R tmpr = u01<R>(w0) * (R)2 * PI_R, sinr, cosr; m_sincos(tmpr, &sinr, &cosr);
+      R r = w * u01<R>(w1);
       f.p0 += r * cosr; f.p1 += r * sinr;
     } break;
     case 35: {
-      R ang = u01<R>(rng.word()) * (R)2 * PI_R, sina, cosa; m_sincos(ang, &sina, &cosa);
-      R g1 = u01<R>(rng.word()), g2 = u01<R>(rng.word()), g3 = u01<R>(rng.word()), g4 = u01<R>(rng.word());
+      R ang = u01<R>(w0) * (R)2 * PI_R, sina, cosa; m_sincos(ang, &sina, &cosa);
+      R g1 = u01<R>(w1), g2 = u01<R>(w2), g3 = u01<R>(w3), g4 = u01<R>(w4);
       R r = w * (g1 + g2 + g3 + g4 - (R)2.0);
       f.p0 += r * cosa; f.p1 += r * sina;
     } break;
     case 36: {
-      R g1 = u01<R>(rng.word()), g2 = u01<R>(rng.word()), g3 = u01<R>(rng.word()), g4 = u01<R>(rng.word());
+      R g1 = u01<R>(w0), g2 = u01<R>(w1), g3 = u01<R>(w2), g4 = u01<R>(w3);
       R rndG = w * (g1 + g2 + g3 + g4 - (R)2.0), sa, ca;
       R ra = f.sqrtv, tmpa = f.atan_yx + P(radialBlur_spinvar) * rndG;
       m_sincos(tmpa, &sa, &ca);
@@ -320,9 +352,9 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
       f.p0 += ra * ca + rz * f.tx; f.p1 += ra * sa + rz * f.ty;
     } break;
     case 37: {
-      int sl = (int)(u01<R>(rng.word()) * P(pie_slices) + (R)0.5);
-      R a = P(pie_rotation) + (R)2.0 * PI_R * ((R)sl + u01<R>(rng.word()) * P(pie_thickness)) / P(pie_slices);
-      R r = w * u01<R>(rng.word()), sa, ca; m_sincos(a, &sa, &ca);
+      int sl = (int)(u01<R>(w0) * P(pie_slices) + (R)0.5);
+      R a = P(pie_rotation) + (R)2.0 * PI_R * ((R)sl + u01<R>(w1) * P(pie_thickness)) / P(pie_slices);
+      R r = w * u01<R>(w2), sa, ca; m_sincos(a, &sa, &ca);
       f.p0 += r * ca; f.p1 += r * sa;
     } break;
     case 38: {
@@ -347,21 +379,21 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
       else f.p1 += w * (((R)2 * m_floor(f.ty / ry) + (R)1) * ry - f.ty);
     } break;
     case 41: {
-      R ang = u01<R>(rng.word()) * w * PI_R, sinr, cosr; m_sincos(ang, &sinr, &cosr);
+      R ang = u01<R>(w0) * w * PI_R, sinr, cosr; m_sincos(ang, &sinr, &cosr);
       f.p0 += w * sinr; f.p1 += w * (sinr * sinr) / cosr;
     } break;
     case 42: f.p0 += w * m_sin(f.tx) / m_cos(f.ty); f.p1 += w * m_tan(f.ty); break;
     case 43: {
-      R a = u01<R>(rng.word()); f.p0 += w * (a - (R)0.5);
-      R b = u01<R>(rng.word()); f.p1 += w * (b - (R)0.5);
+      R a = u01<R>(w0); f.p0 += w * (a - (R)0.5);
+      R b = u01<R>(w1); f.p1 += w * (b - (R)0.5);
     } break;
     case 44: {
-      R ang = w * u01<R>(rng.word()) * PI_R, r = w / (f.sumsq + EPS_R);
+      R ang = w * u01<R>(w0) * PI_R, r = w / (f.sumsq + EPS_R);
       R tanr = w * m_tan(ang) * r;
       f.p0 += tanr * m_cos(f.tx); f.p1 += tanr * m_sin(f.ty);
     } break;
     case 45: {
-      R r = u01<R>(rng.word()) * w * f.sqrtv, sinr, cosr; m_sincos(r, &sinr, &cosr);
+      R r = u01<R>(w0) * w * f.sqrtv, sinr, cosr; m_sincos(r, &sinr, &cosr);
       f.p0 += w * f.tx * (cosr + sinr); f.p1 += w * f.tx * (cosr - sinr);
     } break;
     case 46: {
@@ -370,7 +402,7 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
       if (cr < (R)0) f.p1 += w * (icr + (R)1); else f.p1 += w * (icr - (R)1);
     } break;
     case 47: {
-      R r = u01<R>(rng.word()) * w * f.sqrtv, sinr, cosr; m_sincos(r, &sinr, &cosr);
+      R r = u01<R>(w0) * w * f.sqrtv, sinr, cosr; m_sincos(r, &sinr, &cosr);
       R diff = m_log10(sinr * sinr) + cosr;
       if (badvalue(diff)) diff = (R)-30.0;
       f.p0 += w * f.tx * diff; f.p1 += w * f.tx * (diff - sinr * PI_R);
@@ -388,25 +420,25 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
       R theta = P(super_shape_pm_4) * f.atan_yx + PI_4_R, st, ct; m_sincos(theta, &st, &ct);
       R t1 = m_pow(m_fabs(ct), P(super_shape_n2)), t2 = m_pow(m_fabs(st), P(super_shape_n3));
       R myrnd = P(super_shape_rnd);
-      R r = w * ((myrnd * u01<R>(rng.word()) + ((R)1.0 - myrnd) * f.sqrtv) - P(super_shape_holes)) *
+      R r = w * ((myrnd * u01<R>(w0) + ((R)1.0 - myrnd) * f.sqrtv) - P(super_shape_holes)) *
             m_pow(t1 + t2, P(super_shape_pneg1_n1)) / f.sqrtv;
       f.p0 += r * f.tx; f.p1 += r * f.ty;
     } break;
     case 51: {
       R theta = f.atan_yx;
-      R r = w * (u01<R>(rng.word()) - P(flower_holes)) * m_cos(P(flower_petals) * theta) / f.sqrtv;
+      R r = w * (u01<R>(w0) - P(flower_holes)) * m_cos(P(flower_petals) * theta) / f.sqrtv;
       f.p0 += r * f.tx; f.p1 += r * f.ty;
     } break;
     case 52: {
       R ct = f.tx / f.sqrtv;
-      R r = w * (u01<R>(rng.word()) - P(conic_holes)) * P(conic_eccentricity) /
+      R r = w * (u01<R>(w0) - P(conic_holes)) * P(conic_eccentricity) /
             ((R)1 + P(conic_eccentricity) * ct) / f.sqrtv;
       f.p0 += r * f.tx; f.p1 += r * f.ty;
     } break;
     case 53: {
       R sr, cr; m_sincos(f.sqrtv, &sr, &cr);
-      f.p0 += P(parabola_height) * w * sr * sr * u01<R>(rng.word());
-      f.p1 += P(parabola_width) * w * cr * u01<R>(rng.word());
+      f.p0 += P(parabola_height) * w * sr * sr * u01<R>(w0);
+      f.p1 += P(parabola_width) * w * cr * u01<R>(w1);
     } break;
     case 54: {
       R nx = f.tx, ny = f.ty;
@@ -424,7 +456,7 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
     } break;
     case 56: {
       R roundX = m_rint(f.tx), roundY = m_rint(f.ty), offsetX = f.tx - roundX, offsetY = f.ty - roundY;
-      if (u01<R>(rng.word()) >= (R)0.75) {
+      if (u01<R>(w0) >= (R)0.75) {
         f.p0 += w * (offsetX * (R)0.5 + roundX); f.p1 += w * (offsetY * (R)0.5 + roundY);
       } else if (m_fabs(offsetX) >= m_fabs(offsetY)) {
         if (offsetX >= (R)0.0) {
@@ -463,7 +495,7 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
     case 59: {
       R a = f.atan_yx, lnr = (R)0.5 * m_log(f.sumsq), va = (R)2.0 * PI_R / P(cpow_power);
       R vc = P(cpow_r) / P(cpow_power), vd = P(cpow_i) / P(cpow_power);
-      R ang = vc * a + vd * lnr + va * m_floor(P(cpow_power) * u01<R>(rng.word()));
+      R ang = vc * a + vd * lnr + va * m_floor(P(cpow_power) * u01<R>(w0));
       R sa, ca, m = w * m_exp(vc * lnr - vd * a); m_sincos(ang, &sa, &ca);
       f.p0 += m * ca; f.p1 += m * sa;
     } break;
@@ -581,7 +613,7 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
     } break;
     case 78: {
       R r = w * m_pow(f.sumsq, P(wedgeJulia_cn));
-      int t_rnd = (int)(P(wedgeJulia_rN) * u01<R>(rng.word()));
+      int t_rnd = (int)(P(wedgeJulia_rN) * u01<R>(w0));
       R a = (f.atan_yx + (R)2 * PI_R * (R)t_rnd) / P(wedge_julia_power);
       R c = m_floor((P(wedge_julia_count) * a + PI_R) * ONE_PI_R * (R)0.5), sa, ca;
       a = a * P(wedgeJulia_cf) + c * P(wedge_julia_angle);
@@ -691,9 +723,12 @@ __device__ __noinline__ void var_extended(int v, R w, Helper<R> &f, const XfS<R>
       f.p0 += rad_v * (re_u * re_v + im_u * im_v); f.p1 += rad_v * (im_u * re_v - re_u * im_v);
     } break;
     default:
-      var_basic<R, G>(v, w, f, x, rng);
       break;
   }
+  typename Vec2<R>::T r;
+  r.x = f.p0;
+  r.y = f.p1;
+  return r;
 }
 
 /* variations.c:2129-2399.  p = (x, y, color); q receives (x, y, color,
@@ -731,8 +766,23 @@ __device__ __forceinline__ bool apply_xform(const XfS<R> &x, const uint8_t *var_
   for (int k = 0; k < x.nvars; k++) {
     int v = var_id[x.var_off + k];
     R w = var_w[x.var_off + k];
-    if (FULL && v >= 20) var_extended<R, G>(v, w, f, x, rng);
-    else var_basic<R, G>(v, w, f, x, rng);
+    if (FULL && v >= 20) {
+      /* draw this variation's words first, in its order, then call it */
+      const int nd = ext_draws(v);
+      uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0;
+      if (nd > 0) w0 = rng.word();
+      if (nd > 1) w1 = rng.word();
+      if (nd > 2) w2 = rng.word();
+      if (nd > 3) w3 = rng.word();
+      if (nd > 4) w4 = rng.word();
+      typename Vec2<R>::T r = var_extended_impl<R>(v, w, f.tx, f.ty, f.sumsq, f.sqrtv, f.atan_xy, f.sina, f.cosa,
+                                                   f.atan_yx, f.p0, f.p1, &x, w0, w1, w2, w3, w4);
+      f.p0 = r.x;
+      f.p1 = r.y;
+    } else {
+      const uint32_t rw = (v == 13) ? rng.word() : 0u; /* julia draws one word */
+      var_basic<R>(v, w, f, x, rw);
+    }
   }
   if (x.flags & F3G_F_POST) {
     qx = x.post[0] * f.p0 + x.post[2] * f.p1 + x.post[4];

@@ -1,6 +1,6 @@
 /*
  * f3g_iter_dispatch.cu -- selects the iterate-kernel instantiation for a
- * launch (iteration precision, variation set).
+ * launch (iteration precision, variation set, xform-choice mode).
  */
 #include <cuda_runtime.h>
 
@@ -10,26 +10,37 @@
   extern "C" int f3g_iterate_occ_##tag(int threads);                                                      \
   extern "C" int f3g_iterate_launch_##tag(const F3GPass *, const long long *, int, long long, int, int, int, \
                                           int, F3GCounters *, cudaStream_t);
-DECL(f32b)
-DECL(f32f)
-DECL(f64b)
-DECL(f64f)
+DECL(f32b0)
+DECL(f32b1)
+DECL(f32f0)
+DECL(f32f1)
+DECL(f64b0)
+DECL(f64b1)
+DECL(f64f0)
+DECL(f64f1)
 
-extern "C" int f3g_iterate_occupancy(int precision, int full, int threads) {
-  if (precision == 64) return full ? f3g_iterate_occ_f64f(threads) : f3g_iterate_occ_f64b(threads);
-  return full ? f3g_iterate_occ_f32f(threads) : f3g_iterate_occ_f32b(threads);
+typedef int (*occ_fn)(int);
+typedef int (*launch_fn)(const F3GPass *, const long long *, int, long long, int, int, int, int, F3GCounters *,
+                         cudaStream_t);
+/* index: precision64 * 4 + full * 2 + mode */
+static const occ_fn occ_tab[8] = {f3g_iterate_occ_f32b0, f3g_iterate_occ_f32b1, f3g_iterate_occ_f32f0,
+                                  f3g_iterate_occ_f32f1, f3g_iterate_occ_f64b0, f3g_iterate_occ_f64b1,
+                                  f3g_iterate_occ_f64f0, f3g_iterate_occ_f64f1};
+static const launch_fn launch_tab[8] = {f3g_iterate_launch_f32b0, f3g_iterate_launch_f32b1, f3g_iterate_launch_f32f0,
+                                        f3g_iterate_launch_f32f1, f3g_iterate_launch_f64b0, f3g_iterate_launch_f64b1,
+                                        f3g_iterate_launch_f64f0, f3g_iterate_launch_f64f1};
+
+static int idx(int precision, int full, int mode) {
+  return (precision == 64 ? 4 : 0) + (full ? 2 : 0) + (mode ? 1 : 0);
+}
+
+extern "C" int f3g_iterate_occupancy(int precision, int full, int mode, int threads) {
+  return occ_tab[idx(precision, full, mode)](threads);
 }
 
 extern "C" int f3g_launch_iterate(const F3GPass *d_passes, const long long *d_prefix, int npasses,
-                                  long long total_chunks, int S, int shuffle_every, int precision, int full,
+                                  long long total_chunks, int S, int shuffle_every, int precision, int full, int mode,
                                   int threads, int blocks, F3GCounters *d_ctr, cudaStream_t st) {
-  if (precision == 64)
-    return full ? f3g_iterate_launch_f64f(d_passes, d_prefix, npasses, total_chunks, S, shuffle_every, threads,
-                                          blocks, d_ctr, st)
-                : f3g_iterate_launch_f64b(d_passes, d_prefix, npasses, total_chunks, S, shuffle_every, threads,
-                                          blocks, d_ctr, st);
-  return full ? f3g_iterate_launch_f32f(d_passes, d_prefix, npasses, total_chunks, S, shuffle_every, threads, blocks,
-                                        d_ctr, st)
-              : f3g_iterate_launch_f32b(d_passes, d_prefix, npasses, total_chunks, S, shuffle_every, threads, blocks,
-                                        d_ctr, st);
+  return launch_tab[idx(precision, full, mode)](d_passes, d_prefix, npasses, total_chunks, S, shuffle_every, threads,
+                                                blocks, d_ctr, st);
 }

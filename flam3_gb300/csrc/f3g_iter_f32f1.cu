@@ -1,0 +1,23 @@
+/*
+ * f3g_iter_f32f1.cu -- instantiation of the iterate kernel for FP32 iteration, all variations, warp-coherent xform choice.
+ */
+#include "f3g_iterate.cuh"
+
+extern "C" int f3g_iterate_occ_f32f1(int threads) {
+  int nb = 0;
+  size_t smem = f3g::iterate_smem<float>(threads);
+  if (cudaFuncSetAttribute(f3g::k_iterate<float, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f3g::k_iterate<float, true, 1>, threads, smem) !=
+      cudaSuccess)
+    return 0;
+  return nb;
+}
+
+extern "C" int f3g_iterate_launch_f32f1(const F3GPass *d_passes, const long long *d_prefix, int npasses,
+                                       long long total_chunks, int S, int shuffle_every, int threads, int blocks,
+                                       F3GCounters *d_ctr, cudaStream_t st) {
+  return (int)f3g::launch_iterate_t<float, true, 1>(d_passes, d_prefix, npasses, total_chunks, S, shuffle_every,
+                                                         threads, blocks, d_ctr, st);
+}

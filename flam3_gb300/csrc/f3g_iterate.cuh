@@ -174,31 +174,40 @@ __device__ __forceinline__ unsigned plot(const PassS<R> &s, R qx, R qy, R qc, R 
 }
 
 /* One chain step (flam3.c:249-296).  Returns true when q is a sample to
- * store (false while retrying a bad value). */
+ * store (false while retrying a bad value).  The xform and, when enabled,
+ * the final xform go through one apply_xform call site (a two-stage loop
+ * that is not unrolled) to keep the kernel's code small. */
 template <typename R, bool FULL, class G>
 __device__ __forceinline__ bool chain_step(const PassS<R> &s, int fn, R &px, R &py, R &pc, R &po, int &consec,
                                            int &lastxf, unsigned &bad, R &qx, R &qy, R &qc, R &qo, G &rng) {
-  const XfS<R> &x = s.xf[fn];
-  R nx, ny, nc, no;
-  if (apply_xform<R, FULL, G>(x, s.var_id, s.var_w, px, py, pc, nx, ny, nc, no, rng)) {
-    consec++;
-    bad++;
-    if (consec < 5) {
+  int cur = fn;
+  R ix = px, iy = py, ic = pc;
+#pragma unroll 1
+  for (int stage = 0; stage < 2; stage++) {
+    R nx, ny, nc, no;
+    const bool b = apply_xform<R, FULL, G>(s.xf[cur], s.var_id, s.var_w, ix, iy, ic, nx, ny, nc, no, rng);
+    if (stage == 0) {
+      if (b) {
+        consec++;
+        bad++;
+        if (consec < 5) {
+          px = nx; py = ny; pc = nc; po = no;
+          return false;
+        }
+        consec = 0;
+      } else
+        consec = 0;
+      lastxf = fn + 1;
       px = nx; py = ny; pc = nc; po = no;
-      return false;
-    }
-    consec = 0;
-  } else
-    consec = 0;
-  lastxf = fn + 1;
-  px = nx; py = ny; pc = nc; po = no;
-  qx = px; qy = py; qc = pc; qo = po;
-  if (s.final_enable) {
-    const XfS<R> &fx = s.xf[s.final_index];
-    if (fx.opacity == (R)1 || u01<R>(rng.word()) < fx.opacity) {
-      R fo;
-      apply_xform<R, FULL, G>(fx, s.var_id, s.var_w, px, py, pc, qx, qy, qc, fo, rng);
-      qo = po;
+      qx = px; qy = py; qc = pc; qo = po;
+      if (!s.final_enable) break;
+      const R fop = s.xf[s.final_index].opacity;
+      if (!(fop == (R)1 || u01<R>(rng.word()) < fop)) break;
+      cur = s.final_index;
+      ix = px; iy = py; ic = pc;
+    } else {
+      /* the final xform's result is plotted; the opacity stays the xform's */
+      qx = nx; qy = ny; qc = nc;
     }
   }
   return true;
@@ -275,8 +284,13 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
   bad_total += bad;
 }
 
-template <typename R, bool FULL>
-__global__ void __launch_bounds__(256) k_iterate(const F3GPass *__restrict__ passes,
+/* occupancy target: 3 blocks of 256 threads per SM for FP32 iteration
+ * (85 registers), 2 for FP64 */
+template <typename R> struct IterMinBlocks { static const int v = 3; };
+template <> struct IterMinBlocks<double> { static const int v = 2; };
+
+template <typename R, bool FULL, int MODE>
+__global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GPass *__restrict__ passes,
                                                  const long long *__restrict__ chunk_prefix, int npasses,
                                                  long long total_chunks, int S, int shuffle_every,
                                                  F3GCounters *ctr) {
@@ -315,7 +329,7 @@ __global__ void __launch_bounds__(256) k_iterate(const F3GPass *__restrict__ pas
       __syncthreads();
     }
     long long local = g - chunk_prefix[p];
-    if (s.mode == 1) run_chunk_warp<R, FULL>(s, buf, local, S, shuffle_every, bad, hits);
+    if (MODE == 1) run_chunk_warp<R, FULL>(s, buf, local, S, shuffle_every, bad, hits);
     else run_chunk_thread<R, FULL>(s, local, S, bad, hits);
     __syncthreads();
   }
@@ -331,19 +345,20 @@ __global__ void __launch_bounds__(256) k_iterate(const F3GPass *__restrict__ pas
   }
 }
 
-template <typename R, bool FULL> static size_t iterate_smem(int threads) {
+template <typename R> static size_t iterate_smem(int threads) {
   return ((sizeof(PassS<R>) + 15) & ~(size_t)15) + sizeof(ShufPoint<R>) * (size_t)threads;
 }
 
-template <typename R, bool FULL>
+template <typename R, bool FULL, int MODE>
 static cudaError_t launch_iterate_t(const F3GPass *d_passes, const long long *d_prefix, int npasses,
                                     long long total_chunks, int S, int shuffle_every, int threads, int blocks,
                                     F3GCounters *d_ctr, cudaStream_t st) {
-  size_t smem = iterate_smem<R, FULL>(threads);
-  cudaError_t e = cudaFuncSetAttribute(k_iterate<R, FULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  size_t smem = iterate_smem<R>(threads);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_iterate<R, FULL, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_iterate<R, FULL><<<blocks, threads, smem, st>>>(d_passes, d_prefix, npasses, total_chunks, S, shuffle_every,
-                                                    d_ctr);
+  k_iterate<R, FULL, MODE><<<blocks, threads, smem, st>>>(d_passes, d_prefix, npasses, total_chunks, S,
+                                                          shuffle_every, d_ctr);
   return cudaGetLastError();
 }
 

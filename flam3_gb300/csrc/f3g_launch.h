@@ -6,6 +6,7 @@
 #define F3G_LAUNCH_H
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 
 #include "f3g_common.h"
 
@@ -24,9 +25,9 @@ typedef struct {
   int nchan, transp, bpc;
 } F3GTonemap;
 
-int f3g_iterate_occupancy(int precision, int full, int threads);
+int f3g_iterate_occupancy(int precision, int full, int mode, int threads);
 int f3g_launch_iterate(const F3GPass *d_passes, const long long *d_prefix, int npasses, long long total_chunks,
-                       int S, int shuffle_every, int precision, int full, int threads, int blocks,
+                       int S, int shuffle_every, int precision, int full, int mode, int threads, int blocks,
                        F3GCounters *d_ctr, cudaStream_t st);
 
 int f3g_launch_logscale(const void *buckets, int bkind, long long n, double k1, double k2, void *acc, int akind,
@@ -35,6 +36,11 @@ int f3g_launch_de(const void *buckets, int bkind, const void *count, int W, int 
                   double k2, double curve, int max_filtered_counts, int max_filter_index, int kernel_size,
                   const float *widths, const float *coefs, int R, void *acc, int akind, cudaStream_t st);
 int f3g_de_max_reach(void);
+size_t f3g_de_fused_smem(int oversample, int fw, int R);
+int f3g_launch_de_fused(const void *buckets, int bkind, const void *count, int W, int H, int oversample, double k1,
+                        double k2, double curve, int mfc, int mfi, int ks, const float *widths, const float *coefs,
+                        int R, int de_offset, const float *filter, int fw, int image_w, int image_h,
+                        unsigned char *out, int earlyclip, const F3GTonemap *tp, cudaStream_t st);
 int f3g_launch_earlyclip(void *acc, int akind, long long n, const F3GTonemap *tp, cudaStream_t st);
 int f3g_launch_filter_tonemap(const void *acc, int akind, int W, int de_offset, int oversample, const float *filter,
                               int fw, int image_w, int image_h, unsigned char *out, int earlyclip,

@@ -71,18 +71,26 @@ int f3g_ensure(void **ptr, size_t *cap, size_t need) {
 
 static int ensure_host_passes(f3g_ctx *c, size_t n) {
   size_t need = n * sizeof(F3GPass);
-  if (need <= c->h_passes_bytes && c->h_passes) return 0;
-  if (c->h_passes) cudaFreeHost(c->h_passes);
-  c->h_passes = NULL;
-  if (cudaMallocHost((void **)&c->h_passes, need) != cudaSuccess) {
-    f3g_set_error("cudaMallocHost of %zu bytes failed", need);
+  if (!(need <= c->h_passes_bytes && c->h_passes)) {
+    if (c->h_passes) cudaFreeHost(c->h_passes);
+    c->h_passes = NULL;
     c->h_passes_bytes = 0;
-    return 1;
+    if (cudaMallocHost((void **)&c->h_passes, need) != cudaSuccess) {
+      f3g_set_error("cudaMallocHost of %zu bytes failed", need);
+      return 1;
+    }
+    c->h_passes_bytes = need;
   }
-  c->h_passes_bytes = need;
-  if (c->h_prefix) cudaFreeHost(c->h_prefix);
-  if (cudaMallocHost((void **)&c->h_prefix, (n + 1) * sizeof(long long)) != cudaSuccess) return 1;
-  c->prefix_n = n + 1;
+  if (!(c->h_prefix && c->prefix_n >= n + 1)) {
+    if (c->h_prefix) cudaFreeHost(c->h_prefix);
+    c->h_prefix = NULL;
+    c->prefix_n = 0;
+    if (cudaMallocHost((void **)&c->h_prefix, (n + 1) * sizeof(long long)) != cudaSuccess) {
+      f3g_set_error("cudaMallocHost of the chunk prefix failed");
+      return 1;
+    }
+    c->prefix_n = n + 1;
+  }
   return 0;
 }
 
@@ -344,6 +352,9 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
   double ppux = 0, ppuy = 0, sample_density = 0;
   const int fused_tail = (nbatches == 1) && !(io && io->accum_out);
   int de_used_any = 0;
+  /* fused DE tail state (one batch) */
+  int fde = 0, fde_mfc = 0, fde_mfi = 0, fde_ks = 0, fde_R = 0, fde_count = 0;
+  double fde_k1 = 0, fde_k2 = 0, fde_curve = 0;
 
   for (int batch = 0; batch < nbatches; batch++) {
     double de_time = spec->time + tdeltas[batch * ntemporal];
@@ -418,23 +429,23 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
       for (int ts = 0; ts < ntemporal; ts++) c->h_passes[ts].count = c->d_count;
     }
     if (!(io && io->hist_in)) {
-      int occ = f3g_iterate_occupancy(precision, 1, threads);
+      int full = 0, mode = 1;
+      for (int ts = 0; ts < ntemporal; ts++) {
+        full |= c->h_passes[ts].full_variations;
+        if (c->h_passes[ts].iter_mode == 0) mode = 0;
+      }
+      int occ = f3g_iterate_occupancy(precision, full, mode, threads);
       if (occ < 1) occ = 1;
       int blocks = f3g_opts.blocks > 0 ? f3g_opts.blocks : c->nsm * occ;
       int S = f3g_chunk_samples(c, batch_samples, threads, blocks, spec->sub_batch_size);
-      int full = 0;
       for (int ts = 0; ts < ntemporal; ts++) {
         F3GPass *p = &c->h_passes[ts];
         p->chunk_begin = total_chunks;
         p->nchunks = (p->samples + (long long)threads * S - 1) / ((long long)threads * S);
         total_chunks += p->nchunks;
         c->h_prefix[ts] = p->chunk_begin;
-        full |= p->full_variations;
       }
       c->h_prefix[ntemporal] = total_chunks;
-      occ = f3g_iterate_occupancy(precision, full, threads);
-      if (occ < 1) occ = 1;
-      blocks = f3g_opts.blocks > 0 ? f3g_opts.blocks : c->nsm * occ;
       CK(cudaMemcpyAsync(c->d_passes, c->h_passes, (size_t)ntemporal * sizeof(F3GPass),
                                cudaMemcpyHostToDevice, c->stream));
       h2d += (double)ntemporal * sizeof(F3GPass) + (double)(ntemporal + 1) * sizeof(long long);
@@ -455,8 +466,8 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         h2d += sizeof(F3GCounters);
         d2h += sizeof(F3GCounters);
         CK(cudaEventRecord(c->ev[0], c->stream));
-        int e = f3g_launch_iterate(c->d_passes, c->d_prefix, ntemporal, hi, S, shuffle, precision, full, threads,
-                                   blocks, c->d_ctr, c->stream);
+        int e = f3g_launch_iterate(c->d_passes, c->d_prefix, ntemporal, hi, S, shuffle, precision, full, mode,
+                                   threads, blocks, c->d_ctr, c->stream);
         launches++;
         if (e) {
           f3g_set_error("iterate launch failed: %s", cudaGetErrorString((cudaError_t)e));
@@ -530,10 +541,8 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
     double k2 = (g.oversample * g.oversample * nbatches) / (cp.contrast * area * F3G_WHITE * sample_density * sumfilt);
     if (fused_tail && !de_on) {
       /* the fused tail below reads the histogram directly */
-      c->timings[1] = 0;
       goto tail_fused;
     }
-    CK(cudaEventRecord(c->ev[2], c->stream));
     if (de_on) {
       int R = (int)ceil(de_w[0]) - 1;
       if (R > f3g_de_max_reach()) {
@@ -544,6 +553,23 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
       if (!upload_floats(c, &c->d_de_w, &c->de_w_bytes, de_w, (size_t)nk)) goto done;
       if (!upload_floats(c, &c->d_de_c, &c->de_c_bytes, de_c, (size_t)nk * ks)) goto done;
       h2d += (double)nk * (ks + 1) * sizeof(float);
+      if (fused_tail && f3g_de_fused_smem(g.oversample, g.filter_width, R) <= 220 * 1024) {
+        /* DE, filter, tonemap and pack in one kernel below */
+        fde = 1;
+        fde_mfc = mfc;
+        fde_mfi = mfi;
+        fde_ks = ks;
+        fde_R = R;
+        fde_k1 = k1;
+        fde_k2 = k2;
+        fde_curve = cp.estimator_curve;
+        fde_count = use_count;
+        goto tail_fused;
+      }
+    }
+    CK(cudaEventRecord(c->ev[2], c->stream));
+    if (de_on) {
+      int R = (int)ceil(de_w[0]) - 1;
       int e = f3g_launch_de(c->d_hist, bkind, use_count ? c->d_count : NULL, g.W, g.H, g.oversample, k1, k2,
                             cp.estimator_curve, mfc, mfi, ks, c->d_de_w, c->d_de_c, R, c->d_acc, bkind, c->stream);
       launches++;
@@ -601,7 +627,13 @@ tail_fused:;
     tp.bpc = spec->bytes_per_channel;
     CK(cudaEventRecord(c->ev[4], c->stream));
     int e;
-    if (fused_tail && !de_used_any) {
+    if (fde) {
+      e = f3g_launch_de_fused(c->d_hist, bkind, fde_count ? c->d_count : NULL, g.W, g.H, g.oversample, fde_k1,
+                              fde_k2, fde_curve, fde_mfc, fde_mfi, fde_ks, c->d_de_w, c->d_de_c, fde_R, g.de_offset,
+                              c->d_filter, g.filter_width, g.image_width, g.image_height, c->d_out, spec->earlyclip,
+                              &tp, c->stream);
+      launches++;
+    } else if (fused_tail && !de_used_any) {
       double k1 = (cp.contrast * cp.brightness * 255.0 * 268.0 * 1.0) / 256;
       double area = g.image_width * g.image_height / (ppux * ppuy);
       double k2 = (g.oversample * g.oversample * 1) / (cp.contrast * area * F3G_WHITE * sample_density * sumfilt);
