@@ -48,12 +48,8 @@ struct DEParams {
   F3GTonemap tp;
 };
 
-#define DE_QCAP 768
-
-struct QEntry {
-  int sx, sy, k, reach;
-  float4 v;
-};
+/* sources with more taps than this inside the region go to the warp queue */
+#define DE_WARP_TAPS 32
 
 template <bool FUSED>
 __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
@@ -63,7 +59,8 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
   float *acc = (float *)smem_raw;                 /* 4 planes of A*A */
   float *cnt = acc + 4 * A * A;                   /* Cc*Cc counts / 255 */
   float *filt = cnt + Cc * Cc;                    /* fw*fw (fused) */
-  QEntry *queue = (QEntry *)(((uintptr_t)(filt + P.fw * P.fw) + 15) & ~(uintptr_t)15);
+  /* queue of wide sources: local index in the S x S region, kernel index */
+  uint32_t *queue = (uint32_t *)(filt + P.fw * P.fw);
   __shared__ int qn;
   const int tid = threadIdx.x, nt = blockDim.x;
   /* region origin in bucket coordinates */
@@ -114,16 +111,14 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
     const int x_lo = max(sx - reach, ax0), x_hi = min(sx + reach, ax0 + A - 1);
     const int y_lo = max(sy - reach, ay0), y_hi = min(sy + reach, ay0 + A - 1);
     if (x_lo > x_hi || y_lo > y_hi) continue;
+    const int ntaps = (x_hi - x_lo + 1) * (y_hi - y_lo + 1);
+    if (ntaps > DE_WARP_TAPS) {
+      /* every source fits: the queue has room for the whole S x S region */
+      queue[atomicAdd(&qn, 1)] = ((uint32_t)k << 16) | (uint32_t)fi;
+      continue;
+    }
     const float ls = P.k1 * log1pf(v.w * P.k2) / v.w;
     v = make_float4(v.x * ls, v.y * ls, v.z * ls, v.w * ls);
-    const int ntaps = (x_hi - x_lo + 1) * (y_hi - y_lo + 1);
-    if (ntaps > 16) {
-      int slot = atomicAdd(&qn, 1);
-      if (slot < DE_QCAP) {
-        queue[slot] = QEntry{sx, sy, fi, reach, v};
-        continue;
-      }
-    }
     const float *cf = P.coefs + (long long)fi * P.ks;
     for (int y = y_lo; y <= y_hi; y++) {
       const int ady = abs(y - sy);
@@ -142,25 +137,31 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
   }
   __syncthreads();
   /* queued sources with many taps: one warp each, lanes over the taps */
-  const int nq = min(qn, DE_QCAP);
+  const int nq = qn;
   const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
   for (int q = warp; q < nq; q += nwarps) {
-    const QEntry e = queue[q];
-    const int x_lo = max(e.sx - e.reach, ax0), x_hi = min(e.sx + e.reach, ax0 + A - 1);
-    const int y_lo = max(e.sy - e.reach, ay0), y_hi = min(e.sy + e.reach, ay0 + A - 1);
+    const uint32_t e = queue[q];
+    const int kk = (int)(e >> 16), fi = (int)(e & 0xffffu);
+    const int sx = ax0 - R + kk % S, sy = ay0 - R + kk / S;
+    const int reach = (int)ceilf(__ldg(P.widths + fi)) - 1;
+    float4 v = load_bucket(P.buckets, P.bkind, (long long)sx + (long long)sy * P.W);
+    const float ls = P.k1 * log1pf(v.w * P.k2) / v.w;
+    v = make_float4(v.x * ls, v.y * ls, v.z * ls, v.w * ls);
+    const int x_lo = max(sx - reach, ax0), x_hi = min(sx + reach, ax0 + A - 1);
+    const int y_lo = max(sy - reach, ay0), y_hi = min(sy + reach, ay0 + A - 1);
     const int wdt = x_hi - x_lo + 1, n = wdt * (y_hi - y_lo + 1);
-    const float *cf = P.coefs + (long long)e.k * P.ks;
+    const float *cf = P.coefs + (long long)fi * P.ks;
     for (int t = lane; t < n; t += 32) {
       const int x = x_lo + t % wdt, y = y_lo + t / wdt;
-      const int adx = abs(x - e.sx), ady = abs(y - e.sy);
+      const int adx = abs(x - sx), ady = abs(y - sy);
       const int hi = max(adx, ady), lo = min(adx, ady);
       const float w = __ldg(cf + hi * (hi + 1) / 2 + lo);
       if (w == 0.0f) continue;
       const int o = (x - ax0) + (y - ay0) * A;
-      atomicAdd(acc + o, w * e.v.x);
-      atomicAdd(acc + A * A + o, w * e.v.y);
-      atomicAdd(acc + 2 * A * A + o, w * e.v.z);
-      atomicAdd(acc + 3 * A * A + o, w * e.v.w);
+      atomicAdd(acc + o, w * v.x);
+      atomicAdd(acc + A * A + o, w * v.y);
+      atomicAdd(acc + 2 * A * A + o, w * v.z);
+      atomicAdd(acc + 3 * A * A + o, w * v.w);
     }
   }
   __syncthreads();
@@ -209,9 +210,7 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
 
 static size_t de_smem(int A, int R, int ss, int fw) {
   const int S = A + 2 * R, Cc = S + 2 * ss;
-  size_t b = (size_t)4 * A * A * 4 + (size_t)Cc * Cc * 4 + (size_t)fw * fw * 4;
-  b = (b + 15) & ~(size_t)15;
-  return b + (size_t)DE_QCAP * sizeof(QEntry);
+  return (size_t)4 * A * A * 4 + (size_t)Cc * Cc * 4 + (size_t)fw * fw * 4 + (size_t)S * S * 4;
 }
 
 static DEParams base_params(const void *buckets, int bkind, const void *count, int W, int H, int oversample,
