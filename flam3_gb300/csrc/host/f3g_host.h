@@ -15,6 +15,21 @@
 #define F3_RANDSIZ RANDSIZ
 #endif
 
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* geometry of a render (rect.c:613-687) */
+typedef struct {
+  int oversample, image_width, image_height, out_width;
+  int filter_width, gutter, de_offset, W, H;
+} f3g_geom;
+
+int f3g_geometry(flam3_frame *spec, const flam3_genome *cp, int field, double **filter, f3g_geom *g);
+int f3g_camera(flam3_frame *spec, const flam3_genome *cp, int field, const f3g_geom *g, F3GPass *p,
+               double *sample_density, double *ppux, double *ppuy);
+void f3g_pass_key(flam3_frame *spec, uint32_t key[2]);
+
 /* error reporting: message kept per thread, also printed to stderr */
 void f3g_set_error(const char *fmt, ...);
 void f3g_clear_error(void);
@@ -72,5 +87,9 @@ int f3g_ensure(void **ptr, size_t *cap, size_t need);
 extern flam3gpu_options f3g_opts;
 /* samples per thread per chunk for a pass of `samples` samples */
 int f3g_chunk_samples(const f3g_ctx *c, long long samples, int threads, int blocks, int sub_batch_size);
+
+#ifdef __cplusplus
+}
+#endif
 
 #endif

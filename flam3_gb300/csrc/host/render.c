@@ -105,12 +105,6 @@ int f3g_chunk_samples(const f3g_ctx *c, long long samples, int threads, int bloc
   return (int)per;
 }
 
-/* geometry of a render (rect.c:613-687) */
-typedef struct {
-  int oversample, image_width, image_height, out_width;
-  int filter_width, gutter, de_offset, W, H;
-} f3g_geom;
-
 static int compute_geom(flam3_frame *spec, const flam3_genome *cp, int field, double **filter, f3g_geom *g) {
   g->oversample = cp->spatial_oversample;
   g->image_width = cp->width;
@@ -785,3 +779,15 @@ done:
   f3g_genome_free(&cp);
   return rv;
 }
+
+/* Thin accessors used by the no-allocation entry point (f3g_noalloc.cu). */
+int f3g_geometry(flam3_frame *spec, const flam3_genome *cp, int field, double **filter, f3g_geom *g) {
+  return compute_geom(spec, cp, field, filter, g);
+}
+
+int f3g_camera(flam3_frame *spec, const flam3_genome *cp, int field, const f3g_geom *g, F3GPass *p,
+               double *sample_density, double *ppux, double *ppuy) {
+  return set_camera(spec, cp, field, g, p, sample_density, ppux, ppuy);
+}
+
+void f3g_pass_key(flam3_frame *spec, uint32_t key[2]) { consume_rc(spec, key); }

@@ -5,6 +5,7 @@
 #ifndef FLAM3_GPU_KERNELS_H
 #define FLAM3_GPU_KERNELS_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -64,6 +65,23 @@ int flam3gpu_accumulate_points(flam3_frame *f, int field, const double *points, 
 int flam3gpu_iterate_chains(flam3_genome *cp, int nchains, int n, int fuse,
                             const double *starts, uint64_t seed, double *samples,
                             long *badvals, int precision);
+
+/* flam3gpu_render without device allocation.  No counterpart in the
+ * reference: for callers that cannot call cudaMalloc (inside CUDA-graph
+ * construction, under a host-owned memory pool, with a fixed device-memory
+ * budget).  Same arguments, output and errors as flam3gpu_render, but all
+ * device scratch (histogram, pass tables, filter tables, staged image) comes
+ * from one static device array of flam3gpu_noalloc_capacity() bytes (48 MiB)
+ * that every GPU loading the library holds until exit; it calls no cudaMalloc
+ * or cudaFree and uses the default stream.  Renders of one batch only, and
+ * only those whose scratch fits the array (roughly 1.5 M FP32 or 0.75 M FP64
+ * histogram buckets including the gutter); anything larger returns 1 with an
+ * error naming the sizes.  Calls share the array: each clears the histogram
+ * first, and calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture. */
+int flam3gpu_render_noalloc(flam3_frame *f, void *out, int field, int nchan, int transp, stat_struct *stats);
+size_t flam3gpu_noalloc_capacity(void);
 
 #ifdef __cplusplus
 }
