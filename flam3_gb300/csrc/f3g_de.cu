@@ -35,11 +35,13 @@ struct DEParams {
   const void *count;
   int bkind, W, H, os, ss, scf;
   float scfact, k1, k2, curve;
-  int mfc, mfi, ks, R;
-  const float *widths, *coefs;
+  int mfc, mfi, R;
+  /* per DE kernel k: (c_k, m_k, r2max_k, reach_k) with
+   * coef(dx, dy) = c_k * 2^(m_k * (dx^2 + dy^2)) for dx^2 + dy^2 <= r2max_k */
+  const float4 *kinfo;
   /* tile geometry */
   int A;            /* accumulator region edge (buckets) */
-  int TO;           /* output pixels per tile edge (fused) or core buckets (accumulate) */
+  int TO;           /* output pixels per tile edge (fused) */
   int de_offset, fw, image_w, image_h, earlyclip;
   const float *filter;
   unsigned char *out;
@@ -48,22 +50,26 @@ struct DEParams {
   F3GTonemap tp;
 };
 
-/* sources with more taps than this inside the region go to the warp queue */
-#define DE_WARP_TAPS 32
+/* sources with more taps than this inside the region go to the shared list */
+#define DE_SMALL_TAPS 16
+
+__device__ __forceinline__ float de_coef(float4 ki, int r2) {
+  return (float)r2 <= ki.z ? ki.x * exp2f(ki.y * (float)r2) : 0.0f;
+}
 
 template <bool FUSED>
 __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int A = P.A, R = P.R, ss = P.ss;
-  const int S = A + 2 * R, Cc = S + 2 * ss;
-  float *acc = (float *)smem_raw;                 /* 4 planes of A*A */
-  float *cnt = acc + 4 * A * A;                   /* Cc*Cc counts / 255 */
+  const int S = A + 2 * R, Cc = S + 2 * ss, AA = A * A;
+  const int nk = P.mfi + 1;
+  float4 *kin = (float4 *)smem_raw;               /* nk kernel constants */
+  float *acc = (float *)(kin + nk);               /* 4 planes of A*A */
+  float *cnt = acc + 4 * AA;                      /* Cc*Cc counts / 255 */
   float *filt = cnt + Cc * Cc;                    /* fw*fw (fused) */
-  /* queue of wide sources: local index in the S x S region, kernel index */
-  uint32_t *queue = (uint32_t *)(filt + P.fw * P.fw);
-  __shared__ int qn;
+  uint32_t *list = (uint32_t *)(filt + P.fw * P.fw); /* wide sources: local index << 16 | kernel */
+  __shared__ int nlist;
   const int tid = threadIdx.x, nt = blockDim.x;
-  /* region origin in bucket coordinates */
   int ax0, ay0;
   if (FUSED) {
     ax0 = P.de_offset + blockIdx.x * P.TO * P.os;
@@ -73,30 +79,28 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
     ay0 = blockIdx.y * A;
   }
   const int cx0 = ax0 - R - ss, cy0 = ay0 - R - ss;
-  if (tid == 0) qn = 0;
-  for (int k = tid; k < 4 * A * A; k += nt) acc[k] = 0.0f;
+  if (tid == 0) nlist = 0;
+  for (int k = tid; k < nk; k += nt) kin[k] = P.kinfo[k];
+  for (int k = tid; k < 4 * AA; k += nt) acc[k] = 0.0f;
   if (FUSED)
     for (int k = tid; k < P.fw * P.fw; k += nt) filt[k] = P.filter[k];
-  /* counts of the source region (+ss border) */
   for (int k = tid; k < Cc * Cc; k += nt) {
-    int bx = cx0 + k % Cc, by = cy0 + k / Cc;
+    const int bx = cx0 + k % Cc, by = cy0 + k / Cc;
     float c = 0.0f;
     if (bx >= 0 && bx < P.W && by >= 0 && by < P.H)
       c = load_count(P.buckets, P.bkind, P.count, (long long)bx + (long long)by * P.W) / 255.0f;
     cnt[k] = c;
   }
   __syncthreads();
-  /* DE loop bounds of the reference (rect.c:79-80) */
+  /* DE loop bounds of the reference (rect.c:79-80, 979) */
   const int istart = P.os - 1, iend = P.W - (P.os - 1);
   const int jstart = P.os - 1, jend = min(P.H, (P.os - 1) + (P.H - 2 * (P.os - 1) + 1));
+  /* 1. classify sources; small ones scatter here (shared atomics) */
   for (int k = tid; k < S * S; k += nt) {
     const int lx = k % S, ly = k / S;
     const int sx = ax0 - R + lx, sy = ay0 - R + ly;
     if (sx < istart || sx >= iend || sy < jstart || sy >= jend) continue;
-    const float c_self = cnt[(lx + ss) + (ly + ss) * Cc];
-    if (c_self == 0.0f) continue;
-    float4 v = load_bucket(P.buckets, P.bkind, (long long)sx + (long long)sy * P.W);
-    if (v.w == 0.0f) continue;
+    if (cnt[(lx + ss) + (ly + ss) * Cc] == 0.0f) continue;
     float f = 0.0f;
     for (int jj = -ss; jj <= ss; jj++)
       for (int ii = -ss; ii <= ss; ii++) f += cnt[(lx + ss + ii) + (ly + ss + jj) * Cc];
@@ -106,85 +110,93 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
     else if (f <= 100.0f) fi = (int)ceilf(f) - 1;
     else fi = 100 + (int)floorf(powf(f - 100.0f, P.curve));
     fi = min(max(fi, 0), P.mfi);
-    const int reach = (int)ceilf(__ldg(P.widths + fi)) - 1;
-    /* part of the source's square inside the region */
+    const float4 ki = kin[fi];
+    const int reach = (int)ki.w;
     const int x_lo = max(sx - reach, ax0), x_hi = min(sx + reach, ax0 + A - 1);
     const int y_lo = max(sy - reach, ay0), y_hi = min(sy + reach, ay0 + A - 1);
     if (x_lo > x_hi || y_lo > y_hi) continue;
-    const int ntaps = (x_hi - x_lo + 1) * (y_hi - y_lo + 1);
-    if (ntaps > DE_WARP_TAPS) {
-      /* every source fits: the queue has room for the whole S x S region */
-      queue[atomicAdd(&qn, 1)] = ((uint32_t)k << 16) | (uint32_t)fi;
+    if ((x_hi - x_lo + 1) * (y_hi - y_lo + 1) > DE_SMALL_TAPS) {
+      list[atomicAdd(&nlist, 1)] = ((uint32_t)k << 16) | (uint32_t)fi;
       continue;
     }
+    float4 v = load_bucket(P.buckets, P.bkind, (long long)sx + (long long)sy * P.W);
+    if (v.w == 0.0f) continue;
     const float ls = P.k1 * log1pf(v.w * P.k2) / v.w;
     v = make_float4(v.x * ls, v.y * ls, v.z * ls, v.w * ls);
-    const float *cf = P.coefs + (long long)fi * P.ks;
     for (int y = y_lo; y <= y_hi; y++) {
-      const int ady = abs(y - sy);
+      const int dy = y - sy;
       for (int x = x_lo; x <= x_hi; x++) {
-        const int adx = abs(x - sx);
-        const int hi = max(adx, ady), lo = min(adx, ady);
-        const float w = __ldg(cf + hi * (hi + 1) / 2 + lo);
+        const int dx = x - sx;
+        const float w = de_coef(ki, dx * dx + dy * dy);
         if (w == 0.0f) continue;
         const int o = (x - ax0) + (y - ay0) * A;
         atomicAdd(acc + o, w * v.x);
-        atomicAdd(acc + A * A + o, w * v.y);
-        atomicAdd(acc + 2 * A * A + o, w * v.z);
-        atomicAdd(acc + 3 * A * A + o, w * v.w);
+        atomicAdd(acc + AA + o, w * v.y);
+        atomicAdd(acc + 2 * AA + o, w * v.z);
+        atomicAdd(acc + 3 * AA + o, w * v.w);
       }
     }
   }
   __syncthreads();
-  /* queued sources with many taps: one warp each, lanes over the taps */
-  const int nq = qn;
+  /* 2. wide sources: one warp per source, lanes over its taps inside the
+   * region (row-major; each lane advances by 32 taps without dividing) */
+  const int nl = nlist;
   const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
-  for (int q = warp; q < nq; q += nwarps) {
-    const uint32_t e = queue[q];
+  for (int q = warp; q < nl; q += nwarps) {
+    const uint32_t e = list[q];
     const int kk = (int)(e >> 16), fi = (int)(e & 0xffffu);
     const int sx = ax0 - R + kk % S, sy = ay0 - R + kk / S;
-    const int reach = (int)ceilf(__ldg(P.widths + fi)) - 1;
+    const float4 ki = kin[fi];
+    const int reach = (int)ki.w;
     float4 v = load_bucket(P.buckets, P.bkind, (long long)sx + (long long)sy * P.W);
+    if (v.w == 0.0f) continue;
     const float ls = P.k1 * log1pf(v.w * P.k2) / v.w;
     v = make_float4(v.x * ls, v.y * ls, v.z * ls, v.w * ls);
     const int x_lo = max(sx - reach, ax0), x_hi = min(sx + reach, ax0 + A - 1);
     const int y_lo = max(sy - reach, ay0), y_hi = min(sy + reach, ay0 + A - 1);
-    const int wdt = x_hi - x_lo + 1, n = wdt * (y_hi - y_lo + 1);
-    const float *cf = P.coefs + (long long)fi * P.ks;
-    for (int t = lane; t < n; t += 32) {
-      const int x = x_lo + t % wdt, y = y_lo + t / wdt;
-      const int adx = abs(x - sx), ady = abs(y - sy);
-      const int hi = max(adx, ady), lo = min(adx, ady);
-      const float w = __ldg(cf + hi * (hi + 1) / 2 + lo);
-      if (w == 0.0f) continue;
-      const int o = (x - ax0) + (y - ay0) * A;
-      atomicAdd(acc + o, w * v.x);
-      atomicAdd(acc + A * A + o, w * v.y);
-      atomicAdd(acc + 2 * A * A + o, w * v.z);
-      atomicAdd(acc + 3 * A * A + o, w * v.w);
+    const int wdt = x_hi - x_lo + 1;
+    const int step_y = 32 / wdt, step_x = 32 % wdt;
+    int cx = lane % wdt, y = y_lo + lane / wdt;
+    const int dx0 = x_lo - sx;
+    while (y <= y_hi) {
+      const int dx = dx0 + cx, dy = y - sy;
+      const float w = de_coef(ki, dx * dx + dy * dy);
+      if (w != 0.0f) {
+        const int o = (x_lo - ax0 + cx) + (y - ay0) * A;
+        atomicAdd(acc + o, w * v.x);
+        atomicAdd(acc + AA + o, w * v.y);
+        atomicAdd(acc + 2 * AA + o, w * v.z);
+        atomicAdd(acc + 3 * AA + o, w * v.w);
+      }
+      cx += step_x;
+      y += step_y;
+      if (cx >= wdt) {
+        cx -= wdt;
+        y++;
+      }
     }
   }
   __syncthreads();
   if (!FUSED) {
     /* add the core tile to the global accumulator (tiles do not overlap) */
-    for (int k = tid; k < A * A; k += nt) {
+    for (int k = tid; k < AA; k += nt) {
       const int x = ax0 + k % A, y = ay0 + k / A;
       if (x >= P.W || y >= P.H) continue;
       const long long g = (long long)x + (long long)y * P.W;
       float4 o = acc_load(P.acc, P.akind, g);
       acc_store(P.acc, P.akind, g,
-                make_float4(o.x + acc[k], o.y + acc[A * A + k], o.z + acc[2 * A * A + k], o.w + acc[3 * A * A + k]));
+                make_float4(o.x + acc[k], o.y + acc[AA + k], o.z + acc[2 * AA + k], o.w + acc[3 * AA + k]));
     }
     return;
   }
   if (P.earlyclip) {
-    for (int k = tid; k < A * A; k += nt) {
-      float t[4] = {acc[k], acc[A * A + k], acc[2 * A * A + k], acc[3 * A * A + k]};
+    for (int k = tid; k < AA; k += nt) {
+      float t[4] = {acc[k], acc[AA + k], acc[2 * AA + k], acc[3 * AA + k]};
       tonemap(t, P.tp);
       acc[k] = t[0];
-      acc[A * A + k] = t[1];
-      acc[2 * A * A + k] = t[2];
-      acc[3 * A * A + k] = t[3];
+      acc[AA + k] = t[1];
+      acc[2 * AA + k] = t[2];
+      acc[3 * AA + k] = t[3];
     }
     __syncthreads();
   }
@@ -199,29 +211,28 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
         const float w = filt[ii + jj * P.fw];
         const int o = (lx + ii) + (ly + jj) * A;
         t[0] += w * acc[o];
-        t[1] += w * acc[A * A + o];
-        t[2] += w * acc[2 * A * A + o];
-        t[3] += w * acc[3 * A * A + o];
+        t[1] += w * acc[AA + o];
+        t[2] += w * acc[2 * AA + o];
+        t[3] += w * acc[3 * AA + o];
       }
     if (!P.earlyclip) tonemap(t, P.tp);
     pack_pixel(P.out + (size_t)P.tp.nchan * P.tp.bpc * ((size_t)i + (size_t)j * P.image_w), t, P.tp);
   }
 }
 
-static size_t de_smem(int A, int R, int ss, int fw) {
+static size_t de_smem(int A, int R, int ss, int fw, int nk) {
   const int S = A + 2 * R, Cc = S + 2 * ss;
-  return (size_t)4 * A * A * 4 + (size_t)Cc * Cc * 4 + (size_t)fw * fw * 4 + (size_t)S * S * 4;
+  return (size_t)nk * 16 + (size_t)4 * A * A * 4 + (size_t)Cc * Cc * 4 + (size_t)fw * fw * 4 + (size_t)S * S * 4;
 }
 
 static DEParams base_params(const void *buckets, int bkind, const void *count, int W, int H, int oversample,
-                            double k1, double k2, double curve, int mfc, int mfi, int ks, const float *widths,
-                            const float *coefs, int R) {
+                            double k1, double k2, double curve, int mfc, int mfi, const float4 *kinfo, int R) {
   DEParams P;
   P.buckets = buckets; P.count = count; P.bkind = bkind; P.W = W; P.H = H; P.os = oversample;
   P.ss = oversample / 2; P.scf = !(oversample & 1);
   P.scfact = (float)((oversample / (oversample + 1.0)) * (oversample / (oversample + 1.0)));
   P.k1 = (float)k1; P.k2 = (float)k2; P.curve = (float)curve;
-  P.mfc = mfc; P.mfi = mfi; P.ks = ks; P.R = R; P.widths = widths; P.coefs = coefs;
+  P.mfc = mfc; P.mfi = mfi; P.R = R; P.kinfo = kinfo;
   P.de_offset = 0; P.fw = 0; P.image_w = P.image_h = 0; P.earlyclip = 0; P.filter = nullptr; P.out = nullptr;
   P.acc = nullptr; P.akind = bkind;
   return P;
@@ -231,22 +242,43 @@ static DEParams base_params(const void *buckets, int bkind, const void *count, i
 
 using namespace f3g;
 
-extern "C" size_t f3g_de_fused_smem(int oversample, int fw, int R) {
+/* Per-kernel constants from the reference's tables (filters.c:272-407):
+ * coefs[k][0] is the kernel's value at distance 0 (its normalisation),
+ * widths[k] its radius h_k; the coefficient at squared distance r2 is
+ * coefs[k][0] * exp(-4.5 r2 / h_k^2) inside the disc, and the disc is the set
+ * of (dx, dy) whose table entry is non-zero. */
+extern "C" void f3g_de_kernel_info(int mfi, int ks, const double *widths, const double *coefs, float *out) {
+  for (int k = 0; k <= mfi; k++) {
+    const double h = widths[k];
+    const double *c = coefs + (size_t)k * ks;
+    int r2max = -1, idx = 0, half = 0;
+    while ((half + 1) * (half + 2) / 2 < ks) half++;
+    for (int a = 0; a <= half; a++)
+      for (int b = 0; b <= a; b++, idx++)
+        if (c[idx] != 0.0 && a * a + b * b > r2max) r2max = a * a + b * b;
+    out[4 * k + 0] = (float)c[0];
+    out[4 * k + 1] = (float)(-4.5 / (h * h) / log(2.0));
+    out[4 * k + 2] = (float)r2max;
+    out[4 * k + 3] = (float)(ceil(h) - 1);
+  }
+}
+
+extern "C" size_t f3g_de_fused_smem(int oversample, int fw, int R, int nk) {
   const int TO = 16, A = (TO - 1) * oversample + fw;
-  return de_smem(A, R, oversample / 2, fw);
+  return de_smem(A, R, oversample / 2, fw, nk);
 }
 
 extern "C" int f3g_launch_de_fused(const void *buckets, int bkind, const void *count, int W, int H, int oversample,
-                                   double k1, double k2, double curve, int mfc, int mfi, int ks, const float *widths,
-                                   const float *coefs, int R, int de_offset, const float *filter, int fw,
-                                   int image_w, int image_h, unsigned char *out, int earlyclip, const F3GTonemap *tp,
-                                   cudaStream_t st) {
-  DEParams P = base_params(buckets, bkind, count, W, H, oversample, k1, k2, curve, mfc, mfi, ks, widths, coefs, R);
+                                   double k1, double k2, double curve, int mfc, int mfi, const float *kinfo, int R,
+                                   int de_offset, const float *filter, int fw, int image_w, int image_h,
+                                   unsigned char *out, int earlyclip, const F3GTonemap *tp, cudaStream_t st) {
+  DEParams P = base_params(buckets, bkind, count, W, H, oversample, k1, k2, curve, mfc, mfi,
+                           (const float4 *)kinfo, R);
   P.TO = 16;
   P.A = (P.TO - 1) * oversample + fw;
   P.de_offset = de_offset; P.fw = fw; P.filter = filter; P.image_w = image_w; P.image_h = image_h;
   P.out = out; P.earlyclip = earlyclip; P.tp = *tp;
-  size_t smem = de_smem(P.A, R, P.ss, fw);
+  size_t smem = de_smem(P.A, R, P.ss, fw, mfi + 1);
   if (smem > 220 * 1024) return -1;
   cudaError_t e = cudaFuncSetAttribute(k_de_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
@@ -256,14 +288,15 @@ extern "C" int f3g_launch_de_fused(const void *buckets, int bkind, const void *c
 }
 
 extern "C" int f3g_launch_de(const void *buckets, int bkind, const void *count, int W, int H, int oversample,
-                             double k1, double k2, double curve, int mfc, int mfi, int ks, const float *widths,
-                             const float *coefs, int R, void *acc, int akind, cudaStream_t st) {
-  DEParams P = base_params(buckets, bkind, count, W, H, oversample, k1, k2, curve, mfc, mfi, ks, widths, coefs, R);
+                             double k1, double k2, double curve, int mfc, int mfi, const float *kinfo, int R,
+                             void *acc, int akind, cudaStream_t st) {
+  DEParams P = base_params(buckets, bkind, count, W, H, oversample, k1, k2, curve, mfc, mfi,
+                           (const float4 *)kinfo, R);
   P.A = 32;
   P.TO = 32;
   P.acc = acc;
   P.akind = akind;
-  size_t smem = de_smem(P.A, R, P.ss, 0);
+  size_t smem = de_smem(P.A, R, P.ss, 0, mfi + 1);
   if (smem > 220 * 1024) return -1;
   cudaError_t e = cudaFuncSetAttribute(k_de_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;

@@ -32,15 +32,17 @@ int f3g_launch_iterate(const F3GPass *d_passes, const long long *d_prefix, int n
 
 int f3g_launch_logscale(const void *buckets, int bkind, long long n, double k1, double k2, void *acc, int akind,
                         cudaStream_t st);
+/* DE kernels take per-kernel constants (4 floats per kernel, see f3g_de.cu) */
+void f3g_de_kernel_info(int mfi, int ks, const double *widths, const double *coefs, float *out);
 int f3g_launch_de(const void *buckets, int bkind, const void *count, int W, int H, int oversample, double k1,
-                  double k2, double curve, int max_filtered_counts, int max_filter_index, int kernel_size,
-                  const float *widths, const float *coefs, int R, void *acc, int akind, cudaStream_t st);
+                  double k2, double curve, int max_filtered_counts, int max_filter_index, const float *kinfo, int R,
+                  void *acc, int akind, cudaStream_t st);
 int f3g_de_max_reach(void);
-size_t f3g_de_fused_smem(int oversample, int fw, int R);
+size_t f3g_de_fused_smem(int oversample, int fw, int R, int nk);
 int f3g_launch_de_fused(const void *buckets, int bkind, const void *count, int W, int H, int oversample, double k1,
-                        double k2, double curve, int mfc, int mfi, int ks, const float *widths, const float *coefs,
-                        int R, int de_offset, const float *filter, int fw, int image_w, int image_h,
-                        unsigned char *out, int earlyclip, const F3GTonemap *tp, cudaStream_t st);
+                        double k2, double curve, int mfc, int mfi, const float *kinfo, int R, int de_offset,
+                        const float *filter, int fw, int image_w, int image_h, unsigned char *out, int earlyclip,
+                        const F3GTonemap *tp, cudaStream_t st);
 int f3g_launch_earlyclip(void *acc, int akind, long long n, const F3GTonemap *tp, cudaStream_t st);
 int f3g_launch_filter_tonemap(const void *acc, int akind, int W, int de_offset, int oversample, const float *filter,
                               int fw, int image_w, int image_h, unsigned char *out, int earlyclip,

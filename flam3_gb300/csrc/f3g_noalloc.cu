@@ -149,7 +149,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
                           &de_c);
       if (ks < 0) goto done;
       R = (int)ceil(de_w[0]) - 1;
-      if (mfi > 0 && f3g_de_fused_smem(g.oversample, g.filter_width, R) > 220 * 1024) {
+      if (mfi > 0 && f3g_de_fused_smem(g.oversample, g.filter_width, R, mfi + 1) > 220 * 1024) {
         f3g_set_error("density estimation radius %d is beyond the no-allocation render", R);
         goto done;
       }
@@ -168,7 +168,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
       cv.take((size_t)(ntemporal + 1) * sizeof(long long));
       cv.take(sizeof(F3GCounters));
       cv.take((size_t)g.filter_width * g.filter_width * sizeof(float));
-      cv.take(de_on ? (size_t)(mfi + 1) * (ks + 1) * sizeof(float) : 0);
+      cv.take(de_on ? (size_t)(mfi + 1) * 4 * sizeof(float) : 0);
       cv.take((size_t)nb * bsz);
       cv.take(de_on ? (size_t)nb * csz : 0);
       cv.take(out_bytes);
@@ -184,7 +184,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     long long *d_prefix = (long long *)cv.take((size_t)(ntemporal + 1) * sizeof(long long));
     F3GCounters *d_ctr = (F3GCounters *)cv.take(sizeof(F3GCounters));
     float *d_filter = (float *)cv.take((size_t)g.filter_width * g.filter_width * sizeof(float));
-    float *d_de = (float *)cv.take(de_on ? (size_t)(mfi + 1) * (ks + 1) * sizeof(float) : 0);
+    float *d_de = (float *)cv.take(de_on ? (size_t)(mfi + 1) * 4 * sizeof(float) : 0);
     void *d_hist = cv.take((size_t)nb * bsz);
     void *d_count = cv.take(de_on ? (size_t)nb * csz : 0);
     unsigned char *d_out = (unsigned char *)cv.take(out_bytes);
@@ -192,7 +192,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     /* host tables (host memory only) */
     passes = (F3GPass *)malloc((size_t)ntemporal * sizeof(F3GPass));
     prefix = (long long *)malloc((size_t)(ntemporal + 1) * sizeof(long long));
-    const size_t nf = (size_t)g.filter_width * g.filter_width + (de_on ? (size_t)(mfi + 1) * (ks + 1) : 0);
+    const size_t nf = (size_t)g.filter_width * g.filter_width + (de_on ? (size_t)(mfi + 1) * 4 : 0);
     fbuf = (float *)malloc(nf * sizeof(float));
     if (!passes || !prefix || !fbuf) {
       f3g_set_error("host memory exhausted");
@@ -252,9 +252,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     prefix[ntemporal] = total_chunks;
     for (size_t i = 0; i < (size_t)g.filter_width * g.filter_width; i++) fbuf[i] = (float)filter[i];
     if (de_on) {
-      float *w = fbuf + (size_t)g.filter_width * g.filter_width;
-      for (int i = 0; i <= mfi; i++) w[i] = (float)de_w[i];
-      for (size_t i = 0; i < (size_t)(mfi + 1) * ks; i++) w[mfi + 1 + i] = (float)de_c[i];
+      f3g_de_kernel_info(mfi, ks, de_w, de_c, fbuf + (size_t)g.filter_width * g.filter_width);
     }
     F3GCounters ctr;
     memset(&ctr, 0, sizeof(ctr));
@@ -267,7 +265,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     NCK(cudaMemcpy(d_filter, fbuf, (size_t)g.filter_width * g.filter_width * sizeof(float), cudaMemcpyHostToDevice));
     if (de_on)
       NCK(cudaMemcpy(d_de, fbuf + (size_t)g.filter_width * g.filter_width,
-                     (size_t)(mfi + 1) * (ks + 1) * sizeof(float), cudaMemcpyHostToDevice));
+                     (size_t)(mfi + 1) * 4 * sizeof(float), cudaMemcpyHostToDevice));
     const int shuffle = f3g_opts.shuffle_every > 0 ? f3g_opts.shuffle_every : 1;
     int e = f3g_launch_iterate(d_passes, d_prefix, ntemporal, total_chunks, S, shuffle, precision, full, mode, threads,
                                blocks, d_ctr, 0);
@@ -293,7 +291,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     tp.bpc = spec->bytes_per_channel;
     if (de_on)
       e = f3g_launch_de_fused(d_hist, bkind, use_count ? d_count : nullptr, g.W, g.H, g.oversample, k1, k2,
-                              cp.estimator_curve, mfc, mfi, ks, d_de, d_de + mfi + 1, R, g.de_offset, d_filter,
+                              cp.estimator_curve, mfc, mfi, d_de, R, g.de_offset, d_filter,
                               g.filter_width, g.image_width, g.image_height, d_out, spec->earlyclip, &tp, 0);
     else
       e = f3g_launch_fused_log_filter(d_hist, bkind, g.W, g.H, k1, k2, g.de_offset, g.oversample, d_filter,

@@ -347,7 +347,7 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
   const int fused_tail = (nbatches == 1) && !(io && io->accum_out);
   int de_used_any = 0;
   /* fused DE tail state (one batch) */
-  int fde = 0, fde_mfc = 0, fde_mfi = 0, fde_ks = 0, fde_R = 0, fde_count = 0;
+  int fde = 0, fde_mfc = 0, fde_mfi = 0, fde_R = 0, fde_count = 0;
   double fde_k1 = 0, fde_k2 = 0, fde_curve = 0;
 
   for (int batch = 0; batch < nbatches; batch++) {
@@ -544,15 +544,22 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         goto done;
       }
       int nk = mfi + 1;
-      if (!upload_floats(c, &c->d_de_w, &c->de_w_bytes, de_w, (size_t)nk)) goto done;
-      if (!upload_floats(c, &c->d_de_c, &c->de_c_bytes, de_c, (size_t)nk * ks)) goto done;
-      h2d += (double)nk * (ks + 1) * sizeof(float);
-      if (fused_tail && f3g_de_fused_smem(g.oversample, g.filter_width, R) <= 220 * 1024) {
+      {
+        float *ki = (float *)malloc((size_t)nk * 4 * sizeof(float));
+        double *kid = (double *)malloc((size_t)nk * 4 * sizeof(double));
+        f3g_de_kernel_info(mfi, ks, de_w, de_c, ki);
+        for (int i = 0; i < 4 * nk; i++) kid[i] = ki[i];
+        float *ok = upload_floats(c, &c->d_de_w, &c->de_w_bytes, kid, (size_t)nk * 4);
+        free(ki);
+        free(kid);
+        if (!ok) goto done;
+      }
+      h2d += (double)nk * 4 * sizeof(float);
+      if (fused_tail && f3g_de_fused_smem(g.oversample, g.filter_width, R, nk) <= 220 * 1024) {
         /* DE, filter, tonemap and pack in one kernel below */
         fde = 1;
         fde_mfc = mfc;
         fde_mfi = mfi;
-        fde_ks = ks;
         fde_R = R;
         fde_k1 = k1;
         fde_k2 = k2;
@@ -565,7 +572,7 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
     if (de_on) {
       int R = (int)ceil(de_w[0]) - 1;
       int e = f3g_launch_de(c->d_hist, bkind, use_count ? c->d_count : NULL, g.W, g.H, g.oversample, k1, k2,
-                            cp.estimator_curve, mfc, mfi, ks, c->d_de_w, c->d_de_c, R, c->d_acc, bkind, c->stream);
+                            cp.estimator_curve, mfc, mfi, c->d_de_w, R, c->d_acc, bkind, c->stream);
       launches++;
       if (e) {
         f3g_set_error("density estimation launch failed: %s", cudaGetErrorString((cudaError_t)e));
@@ -623,7 +630,7 @@ tail_fused:;
     int e;
     if (fde) {
       e = f3g_launch_de_fused(c->d_hist, bkind, fde_count ? c->d_count : NULL, g.W, g.H, g.oversample, fde_k1,
-                              fde_k2, fde_curve, fde_mfc, fde_mfi, fde_ks, c->d_de_w, c->d_de_c, fde_R, g.de_offset,
+                              fde_k2, fde_curve, fde_mfc, fde_mfi, c->d_de_w, fde_R, g.de_offset,
                               c->d_filter, g.filter_width, g.image_width, g.image_height, c->d_out, spec->earlyclip,
                               &tp, c->stream);
       launches++;
