@@ -19,7 +19,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + CSRC,
                      "-I" + os.path.join(ROOT, "include")]
-CC_FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-Wall", "-Wno-unused-function", "-I" + os.path.join(ROOT, "include"),
+CC_FLAGS = ["-O2", "-std=gnu11", "-ffp-contract=off", "-fPIC", "-Wall", "-Wno-unused-function", "-I" + os.path.join(ROOT, "include"),
             "-I" + CSRC, "-I" + os.path.join(CUDA_HOME, "include")]
 
 

@@ -61,6 +61,11 @@ def load():
                                                C.POINTER(C.c_int)]
     lib.flam3gpu_iterate_chains.argtypes = [G, C.c_int, C.c_int, C.c_int, dp, C.c_uint64, dp,
                                             C.POINTER(C.c_long), C.c_int]
+    lib.flam3gpu_interpolate.argtypes = [G, C.c_int, C.c_double, C.c_double, G]
+    lib.flam3gpu_free_genome.argtypes = [G]
+    lib.flam3gpu_free_genome.restype = None
+    lib.flam3gpu_set_interpolator.argtypes = [C.c_void_p]
+    lib.flam3gpu_set_interpolator.restype = None
     _LIB = lib
     return lib
 
@@ -185,3 +190,30 @@ def accumulate_points(frame, points, field=0):
                                       C.byref(h)):
         _err(lib, "accumulate_points")
     return hist
+
+
+class InterpolatedGenome:
+    """A flam3_genome produced by flam3gpu_interpolate; owns its xform and
+    chaos storage (released with flam3gpu_free_genome)."""
+
+    def __init__(self, g):
+        self.g = g
+
+    def __del__(self):
+        if _LIB is not None and self.g.xform:
+            _LIB.flam3gpu_free_genome(C.byref(self.g))
+
+
+def interpolate(genomes, time, stagger=0.0):
+    """flam3_interpolate (flam3.c:717-802): the genome at `time` between the
+    control points `genomes` (Genome objects or flam3_genome structs, sorted
+    by time)."""
+    lib = load()
+    structs = [getattr(G, "g", G) for G in genomes]
+    arr = (abi.flam3_genome * len(structs))(*structs)
+    out = abi.flam3_genome()
+    out.final_xform_index = -1
+    if lib.flam3gpu_interpolate(arr, len(structs), float(time), float(stagger), C.byref(out)):
+        _err(lib, "flam3gpu_interpolate")
+    return InterpolatedGenome(out)
+

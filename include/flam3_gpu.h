@@ -253,6 +253,21 @@ void flam3gpu_get_options(flam3gpu_options *o);
  * plotted by the iterate kernels. */
 int flam3gpu_last_timings(double t[8]);
 
+/* Replaces flam3_interpolate (flam3.h:562, flam3.c:717-802): the genome at
+ * `time` between control points cps[0..ncps-1] (sorted by time), with the
+ * reference's alignment (flam3_align), linear or Catmull-Rom blending,
+ * log-polar or linear matrix interpolation, palette blending and xform
+ * stagger.  `result` is overwritten (not freed first); release it with
+ * flam3gpu_free_genome.  Smooth interpolation on the first or last segment
+ * falls back to linear (the reference reads past the control points there).
+ * flam3gpu_render uses this function for frames with several genomes unless
+ * flam3gpu_set_interpolator installed another one, e.g. the reference's own
+ * flam3_interpolate when the caller links it. */
+int flam3gpu_interpolate(flam3_genome *cps, int ncps, double time, double stagger, flam3_genome *result);
+void flam3gpu_free_genome(flam3_genome *g);
+void flam3gpu_set_interpolator(void (*fn)(flam3_genome *cps, int ncps, double time, double stagger,
+                                          flam3_genome *result));
+
 #ifdef __cplusplus
 }
 #endif

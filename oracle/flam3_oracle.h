@@ -72,8 +72,11 @@ typedef struct {
 
 /* rect.c:529-1286 restated.  Honors f->bits (32/33/64), f->nthreads (ISAAC
  * streams and worker threads), f->sub_batch_size, earlyclip,
- * bytes_per_channel, field, nchan, transp.  Multi-genome frames use the
- * interpolation in f3o_interpolate (linear, flam3.c:717-802 subset). */
+ * bytes_per_channel, field, nchan, transp.  Multi-genome frames call the
+ * interpolator installed by f3o_set_interpolator (flam3_interpolate's
+ * arguments, flam3.c:717; nonzero return on failure) once per temporal sample and per batch, as
+ * rect.c:592/726/763 call flam3_interpolate. */
+void f3o_set_interpolator(int (*fn)(flam3_genome *, int, double, double, flam3_genome *));
 int f3o_render(flam3_frame *f, void *out, int field, int nchan, int transp, stat_struct *stats);
 int f3o_render_ex(flam3_frame *f, void *out, int field, int nchan, int transp,
                   stat_struct *stats, f3o_render_io *io);

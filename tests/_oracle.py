@@ -66,8 +66,40 @@ def oracle(fast=False):
     lib.f3o_create_xform_distrib.restype = C.POINTER(C.c_ushort)
     lib.f3o_prepare_precalc_flags.argtypes = [G]
     lib.f3o_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+    lib.f3o_set_interpolator.argtypes = [C.c_void_p]
+    lib.f3o_set_interpolator.restype = None
     _cache[key] = lib
     return lib
+
+
+_INTERP = C.CFUNCTYPE(C.c_int, C.POINTER(abi.flam3_genome), C.c_int, C.c_double, C.c_double,
+                      C.POINTER(abi.flam3_genome))
+
+
+def set_interpolator(which="product", fast=False):
+    """Installs the oracle's multi-genome interpolator: libflam3gpu's
+    flam3gpu_interpolate ("product", pinned against the reference by
+    tests/test_interp_pin.py) or the reference's own flam3_interpolate
+    ("reference", only where oracle/_ref was built)."""
+    lib = oracle(fast)
+    if which == "product":
+        from flam3_gb300 import render
+        gpu = render.load()
+        lib.f3o_set_interpolator(C.cast(gpu.flam3gpu_interpolate, C.c_void_p))
+    else:
+        ref = reference(True)
+        ref.flam3_interpolate.argtypes = [C.POINTER(abi.flam3_genome), C.c_int, C.c_double, C.c_double,
+                                          C.POINTER(abi.flam3_genome)]
+        ref.flam3_interpolate.restype = None
+
+        def call(cps, n, t, stagger, out):
+            ref.flam3_interpolate(cps, n, t, stagger, out)
+            return 0
+
+        cb = _INTERP(call)
+        _cache["ref_interp_cb"] = cb  # keep the thunk alive
+        lib.f3o_set_interpolator(C.cast(cb, C.c_void_p))
+    _cache[("interp", fast)] = which
 
 
 def reference(strict=True):
@@ -97,6 +129,8 @@ def reference(strict=True):
 
 def oracle_render(frame, field=0, nchan=3, transp=0, hist_in=None, want_hist=False, want_accum=False, fast=False):
     lib = oracle(fast)
+    if frame.f.ngenomes > 1 and ("interp", fast) not in _cache:
+        set_interpolator("product", fast)
     out = frame.out_buffer(nchan)
     st = abi.stat_struct()
     io = RenderIO()

@@ -11,8 +11,12 @@ where the reference tree does not exist.
   isaac.npz       irand() words for seeded contexts (isaac.c).
   filters.npz     spatial / DE / temporal filter tables (filters.c).
   abi_offsets.txt struct layout of flam3.h as printed by oracle/abi_offsets.c.
+  interp.npz      flam3_interpolate (flam3.c:717-802) results for the seeded
+                  cases of tests/interp_cases.py, and small multi-genome
+                  (animation / motion blur) renders through flam3_render.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [section ...]
+(sections: variations renders isaac filters abi interp; default all)
 """
 import ctypes as C
 import os
@@ -27,6 +31,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 from flam3_gb300 import abi, genome as gm  # noqa: E402
 import _oracle  # noqa: E402
+import interp_cases  # noqa: E402
 
 OUT = os.path.join(ROOT, "tests", "golden")
 
@@ -133,100 +138,150 @@ def make_render_frame(setting):
         nchan, transp, field
 
 
+# multi-genome renders: name, genome seed, bits, estimator, time, temporal samples, nbatches
+ANIM_SETTINGS = [
+    ("anim_b64_de", 2, 64, 3.0, 40.0, 6, 1),
+    ("anim_b33_t2", 3, 33, 0.0, 85.0, 5, 2),
+    ("anim_b64_edge", 4, 64, 0.0, 0.0, 4, 1),
+]
+
+
+def make_anim_frame(setting):
+    name, seed, bits, est, t, nts, nb = setting
+    gs = gm.config2_genomes(seed, width=96, height=72, quality=20.0, temporal_samples=nts, estimator=est)
+    for G in gs:
+        G.g.nbatches = nb
+    return gm.Frame(gs, bits=bits, nthreads=1, seed="golden-%s" % name, time=t)
+
+
+def make_interp(ref):
+    ref.flam3_interpolate.argtypes = [C.POINTER(abi.flam3_genome), C.c_int, C.c_double, C.c_double,
+                                      C.POINTER(abi.flam3_genome)]
+    ref.flam3_interpolate.restype = None
+    res = {}
+    for ci, (name, gs, queries) in enumerate(interp_cases.cases()):
+        arr = interp_cases.genome_array(gs)
+        for qi, (t, stagger) in enumerate(queries):
+            out = abi.flam3_genome()
+            ref.flam3_interpolate(arr, len(gs), t, stagger, C.byref(out))
+            sc, xf, ch, pal = interp_cases.flatten(out)
+            key = "%s_q%d" % (name, qi)
+            res[key + "_scalars"], res[key + "_xforms"] = sc, xf
+            res[key + "_chaos"], res[key + "_palette"] = ch, pal
+    for s in ANIM_SETTINGS:
+        F = make_anim_frame(s)
+        out = F.out_buffer(3)
+        st = abi.stat_struct()
+        r = ref.flam3_render(C.byref(F.f), out.ctypes.data, 0, 3, 0, C.byref(st))
+        assert r == 0, s
+        res[s[0]] = out
+        res[s[0] + "__iters"] = np.array([st.num_iters, st.badvals])
+    np.savez_compressed(os.path.join(OUT, "interp.npz"), **res)
+
+
 def main():
     ref = _oracle.reference(True)
     if ref is None:
         sys.exit("build the reference first: make -C oracle ref")
     os.makedirs(OUT, exist_ok=True)
+    sections = set(sys.argv[1:]) or {"variations", "renders", "isaac", "filters", "abi", "interp"}
+    if "interp" in sections:
+        make_interp(ref)
 
     # --- variations
-    cases = variation_cases()
-    arrays = {k: [] for k in ("coefs", "post", "var", "params", "color", "color_speed", "opacity", "points",
-                              "words", "q", "bad")}
-    for case in cases:
-        G = genome_from_case(case)
-        q, bad = _oracle.ref_apply_xform(G, 0, case["points"], case["words"])
-        for k in ("coefs", "post", "var", "params", "color", "color_speed", "opacity", "points", "words"):
-            arrays[k].append(case[k])
-        arrays["q"].append(q)
-        arrays["bad"].append(bad)
-    np.savez_compressed(os.path.join(OUT, "variations.npz"), **{k: np.array(v) for k, v in arrays.items()},
-                        param_names=np.array(abi.XFORM_PARAMS))
+    if "variations" in sections:
+        cases = variation_cases()
+        arrays = {k: [] for k in ("coefs", "post", "var", "params", "color", "color_speed", "opacity", "points",
+                                  "words", "q", "bad")}
+        for case in cases:
+            G = genome_from_case(case)
+            q, bad = _oracle.ref_apply_xform(G, 0, case["points"], case["words"])
+            for k in ("coefs", "post", "var", "params", "color", "color_speed", "opacity", "points", "words"):
+                arrays[k].append(case[k])
+            arrays["q"].append(q)
+            arrays["bad"].append(bad)
+        np.savez_compressed(os.path.join(OUT, "variations.npz"), **{k: np.array(v) for k, v in arrays.items()},
+                            param_names=np.array(abi.XFORM_PARAMS))
 
     # --- renders
-    imgs = {}
-    for s in RENDER_SETTINGS:
-        F, nchan, transp, field = make_render_frame(s)
-        out = F.out_buffer(nchan)
-        st = abi.stat_struct()
-        r = ref.flam3_render(C.byref(F.f), out.ctypes.data, field, nchan, transp, C.byref(st))
-        assert r == 0, s
-        imgs[s[0]] = out
-        imgs[s[0] + "__iters"] = np.array([st.num_iters, st.badvals])
-        imgs[s[0] + "__rc"] = np.array([F.f.rc.randrsl[i] for i in range(16)] + [F.f.rc.randcnt], dtype=np.uint64)
-    np.savez_compressed(os.path.join(OUT, "renders.npz"), **imgs)
+    if "renders" in sections:
+        imgs = {}
+        for s in RENDER_SETTINGS:
+            F, nchan, transp, field = make_render_frame(s)
+            out = F.out_buffer(nchan)
+            st = abi.stat_struct()
+            r = ref.flam3_render(C.byref(F.f), out.ctypes.data, field, nchan, transp, C.byref(st))
+            assert r == 0, s
+            imgs[s[0]] = out
+            imgs[s[0] + "__iters"] = np.array([st.num_iters, st.badvals])
+            imgs[s[0] + "__rc"] = np.array([F.f.rc.randrsl[i] for i in range(16)] + [F.f.rc.randcnt], dtype=np.uint64)
+        np.savez_compressed(os.path.join(OUT, "renders.npz"), **imgs)
 
     # --- isaac
-    lib = _oracle.oracle()
-    rows = []
-    for seed in (b"", b"abc", b"flam3-gb300", b"x" * 200):
-        rc = abi.randctx()
-        lib.f3o_init_rc(C.byref(rc), seed)
-        rows.append([lib.f3o_irand(C.byref(rc)) for _ in range(100)])
-    # the reference's own seeding: flam3_init_frame reads isaac_seed from env
-    ref_rows = []
-    for seed in ("", "abc", "flam3-gb300", "x" * 200):
-        env = dict(os.environ, isaac_seed=seed)
-        code = ("import ctypes as C,sys;sys.path.insert(0,%r);from flam3_gb300 import abi;"
-                "L=C.CDLL(%r);f=abi.flam3_frame();L.flam3_init_frame(C.byref(f));"
-                "L.irandinit;print(' '.join(str(f.rc.randrsl[i]) for i in range(16)), f.rc.randcnt)"
-                % (ROOT, os.path.join(_oracle.REF_DIR, "libflam3ref_strict.so")))
-        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, check=True)
-        ref_rows.append([int(t) for t in r.stdout.split()])
-    np.savez_compressed(os.path.join(OUT, "isaac.npz"), oracle_words=np.array(rows, dtype=np.uint64),
-                        ref_init=np.array(ref_rows, dtype=np.uint64))
+    if "isaac" in sections:
+        lib = _oracle.oracle()
+        rows = []
+        for seed in (b"", b"abc", b"flam3-gb300", b"x" * 200):
+            rc = abi.randctx()
+            lib.f3o_init_rc(C.byref(rc), seed)
+            rows.append([lib.f3o_irand(C.byref(rc)) for _ in range(100)])
+        # the reference's own seeding: flam3_init_frame reads isaac_seed from env
+        ref_rows = []
+        for seed in ("", "abc", "flam3-gb300", "x" * 200):
+            env = dict(os.environ, isaac_seed=seed)
+            code = ("import ctypes as C,sys;sys.path.insert(0,%r);from flam3_gb300 import abi;"
+                    "L=C.CDLL(%r);f=abi.flam3_frame();L.flam3_init_frame(C.byref(f));"
+                    "L.irandinit;print(' '.join(str(f.rc.randrsl[i]) for i in range(16)), f.rc.randcnt)"
+                    % (ROOT, os.path.join(_oracle.REF_DIR, "libflam3ref_strict.so")))
+            r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, check=True)
+            ref_rows.append([int(t) for t in r.stdout.split()])
+        np.savez_compressed(os.path.join(OUT, "isaac.npz"), oracle_words=np.array(rows, dtype=np.uint64),
+                            ref_init=np.array(ref_rows, dtype=np.uint64))
 
     # --- filters (reference functions)
-    ref.flam3_create_temporal_filter.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double,
-                                                 C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.POINTER(C.c_double))]
-    ref.flam3_create_temporal_filter.restype = C.c_double
+    if "filters" in sections:
+        ref.flam3_create_temporal_filter.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double,
+                                                     C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.POINTER(C.c_double))]
+        ref.flam3_create_temporal_filter.restype = C.c_double
 
-    class DEHelper(C.Structure):
-        _fields_ = [("max_filtered_counts", C.c_int), ("max_filter_index", C.c_int), ("kernel_size", C.c_int),
-                    ("filter_widths", C.POINTER(C.c_double)), ("filter_coefs", C.POINTER(C.c_double))]
+        class DEHelper(C.Structure):
+            _fields_ = [("max_filtered_counts", C.c_int), ("max_filter_index", C.c_int), ("kernel_size", C.c_int),
+                        ("filter_widths", C.POINTER(C.c_double)), ("filter_coefs", C.POINTER(C.c_double))]
 
-    ref.flam3_create_de_filters.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int]
-    ref.flam3_create_de_filters.restype = DEHelper
-    ref.flam3_create_spatial_filter.argtypes = [C.POINTER(abi.flam3_frame), C.c_int, C.POINTER(C.POINTER(C.c_double))]
-    fil = {}
-    for (rad, mn, curve, ss) in [(9, 0, 0.4, 2), (7, 0, 0.4, 1), (11, 0, 0.4, 2), (3, 0.5, 0.6, 1), (2, 0, 0.4, 3)]:
-        d = ref.flam3_create_de_filters(rad, mn, curve, ss)
-        n = d.max_filter_index + 1
-        key = "de_%g_%g_%g_%d" % (rad, mn, curve, ss)
-        fil[key + "_meta"] = np.array([d.max_filtered_counts, d.max_filter_index, d.kernel_size])
-        fil[key + "_widths"] = np.array([d.filter_widths[i] for i in range(n)])
-        fil[key + "_coefs"] = np.array([d.filter_coefs[i] for i in range(n * d.kernel_size)])
-    for (n, typ, fexp, width) in [(1, 0, 0, 1), (100, 0, 0, 1), (50, 1, 0, 1.5), (40, 2, 1.5, 1), (40, 2, -2, 1)]:
-        tf, td = C.POINTER(C.c_double)(), C.POINTER(C.c_double)()
-        s = ref.flam3_create_temporal_filter(n, typ, fexp, width, C.byref(tf), C.byref(td))
-        key = "tf_%d_%d_%g_%g" % (n, typ, fexp, width)
-        fil[key] = np.array([tf[i] for i in range(n)] + [td[i] for i in range(n)] + [s])
-    for knum in range(14):
-        for (ss, rad, field, aspect) in [(1, 0.5, 0, 1.0), (2, 1.0, 0, 1.0), (3, 0.7, 1, 1.3)]:
-            G = gm.config0_genome(0)
-            G.g.spatial_filter_select = knum
-            G.g.spatial_oversample = ss
-            G.g.spatial_filter_radius = rad
-            F = gm.Frame(G, pixel_aspect_ratio=aspect)
-            fp = C.POINTER(C.c_double)()
-            w = ref.flam3_create_spatial_filter(C.byref(F.f), field, C.byref(fp))
-            fil["sf_%d_%d_%g_%d_%g" % (knum, ss, rad, field, aspect)] = np.array([w] + [fp[i] for i in range(w * w)])
-    np.savez_compressed(os.path.join(OUT, "filters.npz"), **fil)
+        ref.flam3_create_de_filters.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int]
+        ref.flam3_create_de_filters.restype = DEHelper
+        ref.flam3_create_spatial_filter.argtypes = [C.POINTER(abi.flam3_frame), C.c_int, C.POINTER(C.POINTER(C.c_double))]
+        fil = {}
+        for (rad, mn, curve, ss) in [(9, 0, 0.4, 2), (7, 0, 0.4, 1), (11, 0, 0.4, 2), (3, 0.5, 0.6, 1), (2, 0, 0.4, 3)]:
+            d = ref.flam3_create_de_filters(rad, mn, curve, ss)
+            n = d.max_filter_index + 1
+            key = "de_%g_%g_%g_%d" % (rad, mn, curve, ss)
+            fil[key + "_meta"] = np.array([d.max_filtered_counts, d.max_filter_index, d.kernel_size])
+            fil[key + "_widths"] = np.array([d.filter_widths[i] for i in range(n)])
+            fil[key + "_coefs"] = np.array([d.filter_coefs[i] for i in range(n * d.kernel_size)])
+        for (n, typ, fexp, width) in [(1, 0, 0, 1), (100, 0, 0, 1), (50, 1, 0, 1.5), (40, 2, 1.5, 1), (40, 2, -2, 1)]:
+            tf, td = C.POINTER(C.c_double)(), C.POINTER(C.c_double)()
+            s = ref.flam3_create_temporal_filter(n, typ, fexp, width, C.byref(tf), C.byref(td))
+            key = "tf_%d_%d_%g_%g" % (n, typ, fexp, width)
+            fil[key] = np.array([tf[i] for i in range(n)] + [td[i] for i in range(n)] + [s])
+        for knum in range(14):
+            for (ss, rad, field, aspect) in [(1, 0.5, 0, 1.0), (2, 1.0, 0, 1.0), (3, 0.7, 1, 1.3)]:
+                G = gm.config0_genome(0)
+                G.g.spatial_filter_select = knum
+                G.g.spatial_oversample = ss
+                G.g.spatial_filter_radius = rad
+                F = gm.Frame(G, pixel_aspect_ratio=aspect)
+                fp = C.POINTER(C.c_double)()
+                w = ref.flam3_create_spatial_filter(C.byref(F.f), field, C.byref(fp))
+                fil["sf_%d_%d_%g_%d_%g" % (knum, ss, rad, field, aspect)] = np.array([w] + [fp[i] for i in range(w * w)])
+        np.savez_compressed(os.path.join(OUT, "filters.npz"), **fil)
 
     # --- ABI
-    r = subprocess.run([os.path.join(_oracle.REF_DIR, "abi_offsets")], capture_output=True, text=True, check=True)
-    with open(os.path.join(OUT, "abi_offsets.txt"), "w") as f:
-        f.write(r.stdout)
+    if "abi" in sections:
+        r = subprocess.run([os.path.join(_oracle.REF_DIR, "abi_offsets")], capture_output=True, text=True, check=True)
+        with open(os.path.join(OUT, "abi_offsets.txt"), "w") as f:
+            f.write(r.stdout)
+
     print("golden fixtures written to", OUT)
 
 

@@ -116,3 +116,20 @@ def test_bits64_render_close_to_bits33(gpulib):
     a, _ = render.render(gm.Frame(cfg0(q=100.0), bits=33, seed="x"))
     b, _ = render.render(gm.Frame(cfg0(q=100.0), bits=64, seed="x"))
     assert mae(a, b) < 0.5
+
+
+def anim_frame(t, nts, est, q=400.0, bits=33, nthreads=8, rc_seed="anim", w=160, h=120):
+    gs = gm.config2_genomes(2, width=w, height=h, quality=q, temporal_samples=nts, estimator=est)
+    return gm.Frame(gs, bits=bits, nthreads=nthreads, seed=rc_seed, time=t)
+
+
+@pytest.mark.parametrize("t,nts,est,bits", [(40.0, 8, 3.0, 33), (119.8, 4, 0.0, 64), (0.0, 3, 0.0, 33)])
+def test_animation_render_close_to_oracle(gpulib, t, nts, est, bits):
+    """Two key genomes, a frame between them with temporal samples (motion
+    blur): every temporal sample interpolates its own genome."""
+    Fo = anim_frame(t, nts, est, bits=bits)
+    o, so, _ = _oracle.oracle_render(Fo)
+    Fg = anim_frame(t, nts, est, bits=bits, rc_seed="anim-g")
+    g, sg = render.render(Fg)
+    assert sg.num_iters == so.num_iters
+    assert mae(o, g) < 2.5, mae(o, g)
