@@ -6,9 +6,10 @@
  * interpolated at that time, prepared (active-variation lists, precalc
  * values, xform-choice table), its colour map scaled by the temporal filter
  * weight, the camera, the number of samples and the histogram it adds to.
- * The iterate kernel processes any list of passes in one persistent launch:
- * work is split into chunks of blockDim*S samples, a block takes chunks from
- * a global counter and stages the pass it belongs to in shared memory.
+ * The iterate kernel processes any list of passes (of any number of renders)
+ * in one persistent launch: work is split into chunks of blockDim*S samples,
+ * a block takes chunks from a global counter and stages the pass it belongs
+ * to in shared memory.
  */
 #ifndef F3G_COMMON_H
 #define F3G_COMMON_H
@@ -117,14 +118,25 @@ typedef struct {
   void *buckets;
   void *count;              /* optional count plane, NULL if A == count */
   int bucket_kind;
-  int pad2;
+  int S;                    /* samples per thread per chunk: a chunk is blockDim*S samples */
+  unsigned long long *counters; /* [0] bad values, [1] samples plotted (device) */
 } F3GPass;
+
+/* One entry of an iterate launch's work list: chunks [chunk_first,
+ * chunk_first + n) of a pass, where n is the entry's span in the launch's
+ * chunk prefix.  Chunk k of a pass always draws the same random stream, so a
+ * pass may be split over several launches (rounds of a batched or served
+ * workload) without changing its samples. */
+typedef struct {
+  const F3GPass *pass;
+  long long chunk_first;
+} F3GItem;
 
 /* Device result counters of one iterate launch. */
 typedef struct {
   unsigned long long next_chunk;  /* work counter */
-  unsigned long long badvals;
-  unsigned long long plotted;
+  unsigned long long badvals;     /* bad values and samples plotted, when a */
+  unsigned long long plotted;     /* pass's counters point here */
   unsigned long long error;       /* nonzero: a kernel refused its input */
 } F3GCounters;
 

@@ -263,28 +263,59 @@ extern "C" void f3g_de_kernel_info(int mfi, int ks, const double *widths, const 
   }
 }
 
-extern "C" size_t f3g_de_fused_smem(int oversample, int fw, int R, int nk) {
-  const int TO = 16, A = (TO - 1) * oversample + fw;
+/* The tail kernels may be launched inside stream capture, where only
+ * stream-ordered calls belong: their shared-memory limit is raised once, to
+ * the largest size any launch asks for, before the first launch. */
+#define DE_SMEM_MAX (220 * 1024)
+template <bool FUSED> static cudaError_t de_attr_once() {
+  static volatile int done = 0;
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_de_tile<FUSED>, cudaFuncAttributeMaxDynamicSharedMemorySize, DE_SMEM_MAX);
+  if (e == cudaSuccess) done = 1;
+  return e;
+}
+
+extern "C" int f3g_de_prepare(void) {
+  cudaError_t e = de_attr_once<true>();
+  if (e == cudaSuccess) e = de_attr_once<false>();
+  return (int)e;
+}
+
+extern "C" size_t f3g_de_fused_smem_tile(int oversample, int fw, int R, int nk, int tile) {
+  const int A = (tile - 1) * oversample + fw;
   return de_smem(A, R, oversample / 2, fw, nk);
+}
+
+extern "C" size_t f3g_de_fused_smem(int oversample, int fw, int R, int nk) {
+  return f3g_de_fused_smem_tile(oversample, fw, R, nk, 16);
+}
+
+extern "C" int f3g_launch_de_fused_tile(const void *buckets, int bkind, const void *count, int W, int H,
+                                        int oversample, double k1, double k2, double curve, int mfc, int mfi,
+                                        const float *kinfo, int R, int de_offset, const float *filter, int fw,
+                                        int image_w, int image_h, unsigned char *out, int earlyclip,
+                                        const F3GTonemap *tp, int tile, cudaStream_t st) {
+  DEParams P = base_params(buckets, bkind, count, W, H, oversample, k1, k2, curve, mfc, mfi,
+                           (const float4 *)kinfo, R);
+  P.TO = tile;
+  P.A = (P.TO - 1) * oversample + fw;
+  P.de_offset = de_offset; P.fw = fw; P.filter = filter; P.image_w = image_w; P.image_h = image_h;
+  P.out = out; P.earlyclip = earlyclip; P.tp = *tp;
+  size_t smem = de_smem(P.A, R, P.ss, fw, mfi + 1);
+  if (tile < 4 || tile > 64 || smem > DE_SMEM_MAX) return -1;
+  cudaError_t e = de_attr_once<true>();
+  if (e != cudaSuccess) return (int)e;
+  dim3 grid((image_w + P.TO - 1) / P.TO, (image_h + P.TO - 1) / P.TO);
+  k_de_tile<true><<<grid, 256, smem, st>>>(P);
+  return (int)cudaGetLastError();
 }
 
 extern "C" int f3g_launch_de_fused(const void *buckets, int bkind, const void *count, int W, int H, int oversample,
                                    double k1, double k2, double curve, int mfc, int mfi, const float *kinfo, int R,
                                    int de_offset, const float *filter, int fw, int image_w, int image_h,
                                    unsigned char *out, int earlyclip, const F3GTonemap *tp, cudaStream_t st) {
-  DEParams P = base_params(buckets, bkind, count, W, H, oversample, k1, k2, curve, mfc, mfi,
-                           (const float4 *)kinfo, R);
-  P.TO = 16;
-  P.A = (P.TO - 1) * oversample + fw;
-  P.de_offset = de_offset; P.fw = fw; P.filter = filter; P.image_w = image_w; P.image_h = image_h;
-  P.out = out; P.earlyclip = earlyclip; P.tp = *tp;
-  size_t smem = de_smem(P.A, R, P.ss, fw, mfi + 1);
-  if (smem > 220 * 1024) return -1;
-  cudaError_t e = cudaFuncSetAttribute(k_de_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return (int)e;
-  dim3 grid((image_w + P.TO - 1) / P.TO, (image_h + P.TO - 1) / P.TO);
-  k_de_tile<true><<<grid, 256, smem, st>>>(P);
-  return (int)cudaGetLastError();
+  return f3g_launch_de_fused_tile(buckets, bkind, count, W, H, oversample, k1, k2, curve, mfc, mfi, kinfo, R,
+                                  de_offset, filter, fw, image_w, image_h, out, earlyclip, tp, 16, st);
 }
 
 extern "C" int f3g_launch_de(const void *buckets, int bkind, const void *count, int W, int H, int oversample,
@@ -297,8 +328,8 @@ extern "C" int f3g_launch_de(const void *buckets, int bkind, const void *count, 
   P.acc = acc;
   P.akind = akind;
   size_t smem = de_smem(P.A, R, P.ss, 0, mfi + 1);
-  if (smem > 220 * 1024) return -1;
-  cudaError_t e = cudaFuncSetAttribute(k_de_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > DE_SMEM_MAX) return -1;
+  cudaError_t e = de_attr_once<false>();
   if (e != cudaSuccess) return (int)e;
   dim3 grid((W + P.A - 1) / P.A, (H + P.A - 1) / P.A);
   k_de_tile<false><<<grid, 256, smem, st>>>(P);

@@ -15,9 +15,9 @@ extern "C" int f3g_iterate_occ_f64b1(int threads) {
   return nb;
 }
 
-extern "C" int f3g_iterate_launch_f64b1(const F3GPass *d_passes, const long long *d_prefix, int npasses,
-                                       long long total_chunks, int S, int shuffle_every, int threads, int blocks,
+extern "C" int f3g_iterate_launch_f64b1(const F3GItem *d_items, const long long *d_prefix, int nitems,
+                                       long long total_chunks, int shuffle_every, int threads, int blocks,
                                        F3GCounters *d_ctr, cudaStream_t st) {
-  return (int)f3g::launch_iterate_t<double, false, 1>(d_passes, d_prefix, npasses, total_chunks, S, shuffle_every,
-                                                         threads, blocks, d_ctr, st);
+  return (int)f3g::launch_iterate_t<double, false, 1>(d_items, d_prefix, nitems, total_chunks, shuffle_every, threads,
+                                                         blocks, d_ctr, st);
 }

@@ -34,8 +34,9 @@ namespace f3g {
 
 template <typename R> struct PassS {
   int num_xforms, num_std, final_index, final_enable, chaos_enable, fuse, mode, full;
-  int width, height, rotate, cmap_size, palette_mode, bucket_kind;
+  int width, height, rotate, cmap_size, palette_mode, bucket_kind, S;
   long long samples, nchunks;
+  unsigned long long *counters;
   uint32_t key0, key1;
   R b0, b1, b2, b3, r00, r01, r10, r11, rcx, rcy, ws0, wb0s0, hs1, hb1s1;
   double db0, db1, db2, db3, dws0, dwb0s0, dhs1, dhb1s1;
@@ -68,6 +69,7 @@ __device__ void stage_pass(PassS<R> &s, const F3GPass *__restrict__ p) {
     s.ws0 = (R)p->ws0; s.wb0s0 = (R)p->wb0s0; s.hs1 = (R)p->hs1; s.hb1s1 = (R)p->hb1s1;
     s.dws0 = p->ws0; s.dwb0s0 = p->wb0s0; s.dhs1 = p->hs1; s.dhb1s1 = p->hb1s1;
     s.buckets = p->buckets; s.count = p->count;
+    s.S = p->S; s.counters = p->counters;
   }
   const int nx = p->num_xforms;
   const int rows = p->num_std + 1;
@@ -289,17 +291,31 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
 template <typename R> struct IterMinBlocks { static const int v = 3; };
 template <> struct IterMinBlocks<double> { static const int v = 2; };
 
+/* add this block's bad-value and plotted counts to the pass's counters */
+__device__ __forceinline__ void flush_counts(unsigned long long *counters, unsigned &bad, unsigned &hits) {
+  unsigned long long b = bad, h = hits;
+  for (int o = 16; o > 0; o >>= 1) {
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    h += __shfl_down_sync(0xffffffffu, h, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (b) atomicAdd(&counters[0], b);
+    if (h) atomicAdd(&counters[1], h);
+  }
+  bad = hits = 0;
+}
+
 template <typename R, bool FULL, int MODE>
-__global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GPass *__restrict__ passes,
-                                                 const long long *__restrict__ chunk_prefix, int npasses,
-                                                 long long total_chunks, int S, int shuffle_every,
-                                                 F3GCounters *ctr) {
+__global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GItem *__restrict__ items,
+                                                 const long long *__restrict__ chunk_prefix, int nitems,
+                                                 long long total_chunks, int shuffle_every, F3GCounters *ctr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   PassS<R> &s = *reinterpret_cast<PassS<R> *>(smem_raw);
   ShufPoint<R> *buf = reinterpret_cast<ShufPoint<R> *>(smem_raw + ((sizeof(PassS<R>) + 15) & ~(size_t)15));
   __shared__ long long sh_chunk;
-  __shared__ int sh_pass;
+  __shared__ int sh_item;
   int cur = -1;
+  long long first = 0;
   unsigned bad = 0, hits = 0;
   for (;;) {
     if (threadIdx.x == 0) {
@@ -307,7 +323,7 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GP
       int p = cur;
       if (g < total_chunks) {
         if (p < 0 || g < chunk_prefix[p] || g >= chunk_prefix[p + 1]) {
-          int lo = 0, hi = npasses - 1;
+          int lo = 0, hi = nitems - 1;
           while (lo < hi) {
             int mid = (lo + hi + 1) >> 1;
             if (chunk_prefix[mid] <= g) lo = mid;
@@ -317,32 +333,26 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GP
         }
       }
       sh_chunk = g;
-      sh_pass = p;
+      sh_item = p;
     }
     __syncthreads();
     long long g = sh_chunk;
-    int p = sh_pass;
+    int p = sh_item;
     if (g >= total_chunks) break;
     if (p != cur) {
-      stage_pass<R>(s, passes + p);
+      if (cur >= 0) flush_counts(s.counters, bad, hits);
+      __syncthreads();
+      stage_pass<R>(s, items[p].pass);
+      first = items[p].chunk_first;
       cur = p;
       __syncthreads();
     }
-    long long local = g - chunk_prefix[p];
-    if (MODE == 1) run_chunk_warp<R, FULL>(s, buf, local, S, shuffle_every, bad, hits);
-    else run_chunk_thread<R, FULL>(s, local, S, bad, hits);
+    long long local = g - chunk_prefix[p] + first;
+    if (MODE == 1) run_chunk_warp<R, FULL>(s, buf, local, s.S, shuffle_every, bad, hits);
+    else run_chunk_thread<R, FULL>(s, local, s.S, bad, hits);
     __syncthreads();
   }
-  /* badvals: warp reduce then one atomic per warp */
-  unsigned long long h = hits;
-  for (int o = 16; o > 0; o >>= 1) {
-    bad += __shfl_down_sync(0xffffffffu, bad, o);
-    h += __shfl_down_sync(0xffffffffu, h, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (bad) atomicAdd(&ctr->badvals, (unsigned long long)bad);
-    if (h) atomicAdd(&ctr->plotted, h);
-  }
+  if (cur >= 0) flush_counts(s.counters, bad, hits);
 }
 
 template <typename R> static size_t iterate_smem(int threads) {
@@ -350,15 +360,15 @@ template <typename R> static size_t iterate_smem(int threads) {
 }
 
 template <typename R, bool FULL, int MODE>
-static cudaError_t launch_iterate_t(const F3GPass *d_passes, const long long *d_prefix, int npasses,
-                                    long long total_chunks, int S, int shuffle_every, int threads, int blocks,
+static cudaError_t launch_iterate_t(const F3GItem *d_items, const long long *d_prefix, int nitems,
+                                    long long total_chunks, int shuffle_every, int threads, int blocks,
                                     F3GCounters *d_ctr, cudaStream_t st) {
   size_t smem = iterate_smem<R>(threads);
   cudaError_t e =
       cudaFuncSetAttribute(k_iterate<R, FULL, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_iterate<R, FULL, MODE><<<blocks, threads, smem, st>>>(d_passes, d_prefix, npasses, total_chunks, S,
-                                                          shuffle_every, d_ctr);
+  k_iterate<R, FULL, MODE><<<blocks, threads, smem, st>>>(d_items, d_prefix, nitems, total_chunks, shuffle_every,
+                                                          d_ctr);
   return cudaGetLastError();
 }
 

@@ -26,8 +26,12 @@ typedef struct {
 } F3GTonemap;
 
 int f3g_iterate_occupancy(int precision, int full, int mode, int threads);
-int f3g_launch_iterate(const F3GPass *d_passes, const long long *d_prefix, int npasses, long long total_chunks,
-                       int S, int shuffle_every, int precision, int full, int mode, int threads, int blocks,
+/* One persistent iterate launch over a work list: item i covers chunk-prefix
+ * span [d_prefix[i], d_prefix[i+1]) of the launch, starting at chunk
+ * d_items[i].chunk_first of its pass.  d_ctr->next_chunk must hold the first
+ * chunk of the launch (normally 0). */
+int f3g_launch_iterate(const F3GItem *d_items, const long long *d_prefix, int nitems, long long total_chunks,
+                       int shuffle_every, int precision, int full, int mode, int threads, int blocks,
                        F3GCounters *d_ctr, cudaStream_t st);
 
 int f3g_launch_logscale(const void *buckets, int bkind, long long n, double k1, double k2, void *acc, int akind,
@@ -43,6 +47,15 @@ int f3g_launch_de_fused(const void *buckets, int bkind, const void *count, int W
                         double k2, double curve, int mfc, int mfi, const float *kinfo, int R, int de_offset,
                         const float *filter, int fw, int image_w, int image_h, unsigned char *out, int earlyclip,
                         const F3GTonemap *tp, cudaStream_t st);
+/* the fused DE kernel with a chosen output-tile edge (tile x tile pixels per block) */
+size_t f3g_de_fused_smem_tile(int oversample, int fw, int R, int nk, int tile);
+int f3g_launch_de_fused_tile(const void *buckets, int bkind, const void *count, int W, int H, int oversample,
+                             double k1, double k2, double curve, int mfc, int mfi, const float *kinfo, int R,
+                             int de_offset, const float *filter, int fw, int image_w, int image_h,
+                             unsigned char *out, int earlyclip, const F3GTonemap *tp, int tile, cudaStream_t st);
+/* raises the tail kernels' shared-memory limits (call before stream capture) */
+int f3g_de_prepare(void);
+int f3g_tail_prepare(void);
 int f3g_launch_earlyclip(void *acc, int akind, long long n, const F3GTonemap *tp, cudaStream_t st);
 int f3g_launch_filter_tonemap(const void *acc, int akind, int W, int de_offset, int oversample, const float *filter,
                               int fw, int image_w, int image_h, unsigned char *out, int earlyclip,

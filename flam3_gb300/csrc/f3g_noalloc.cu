@@ -95,6 +95,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
   float *fbuf = nullptr;
   F3GPass *passes = nullptr;
   long long *prefix = nullptr;
+  F3GItem *items = nullptr;
   flam3_genome cp;
   memset(&cp, 0, sizeof(cp));
   unsigned char *scratch = nullptr;
@@ -166,6 +167,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
       cv.used = 0;
       cv.take((size_t)ntemporal * sizeof(F3GPass));
       cv.take((size_t)(ntemporal + 1) * sizeof(long long));
+      cv.take((size_t)ntemporal * sizeof(F3GItem));
       cv.take(sizeof(F3GCounters));
       cv.take((size_t)g.filter_width * g.filter_width * sizeof(float));
       cv.take(de_on ? (size_t)(mfi + 1) * 4 * sizeof(float) : 0);
@@ -182,6 +184,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     cv.used = 0;
     F3GPass *d_passes = (F3GPass *)cv.take((size_t)ntemporal * sizeof(F3GPass));
     long long *d_prefix = (long long *)cv.take((size_t)(ntemporal + 1) * sizeof(long long));
+    F3GItem *d_items = (F3GItem *)cv.take((size_t)ntemporal * sizeof(F3GItem));
     F3GCounters *d_ctr = (F3GCounters *)cv.take(sizeof(F3GCounters));
     float *d_filter = (float *)cv.take((size_t)g.filter_width * g.filter_width * sizeof(float));
     float *d_de = (float *)cv.take(de_on ? (size_t)(mfi + 1) * 4 * sizeof(float) : 0);
@@ -192,9 +195,10 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     /* host tables (host memory only) */
     passes = (F3GPass *)malloc((size_t)ntemporal * sizeof(F3GPass));
     prefix = (long long *)malloc((size_t)(ntemporal + 1) * sizeof(long long));
+    items = (F3GItem *)malloc((size_t)ntemporal * sizeof(F3GItem));
     const size_t nf = (size_t)g.filter_width * g.filter_width + (de_on ? (size_t)(mfi + 1) * 4 : 0);
     fbuf = (float *)malloc(nf * sizeof(float));
-    if (!passes || !prefix || !fbuf) {
+    if (!passes || !prefix || !items || !fbuf) {
       f3g_set_error("host memory exhausted");
       goto done;
     }
@@ -244,6 +248,10 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     long long total_chunks = 0;
     for (int ts = 0; ts < ntemporal; ts++) {
       passes[ts].count = use_count ? d_count : nullptr;
+      passes[ts].S = S;
+      passes[ts].counters = &d_ctr->badvals;
+      items[ts].pass = d_passes + ts;
+      items[ts].chunk_first = 0;
       passes[ts].chunk_begin = total_chunks;
       passes[ts].nchunks = (passes[ts].samples + (long long)threads * S - 1) / ((long long)threads * S);
       prefix[ts] = total_chunks;
@@ -261,13 +269,14 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     if (use_count) NCK(cudaMemsetAsync(d_count, 0, (size_t)nb * csz, 0));
     NCK(cudaMemcpy(d_passes, passes, (size_t)ntemporal * sizeof(F3GPass), cudaMemcpyHostToDevice));
     NCK(cudaMemcpy(d_prefix, prefix, (size_t)(ntemporal + 1) * sizeof(long long), cudaMemcpyHostToDevice));
+    NCK(cudaMemcpy(d_items, items, (size_t)ntemporal * sizeof(F3GItem), cudaMemcpyHostToDevice));
     NCK(cudaMemcpy(d_ctr, &ctr, sizeof(ctr), cudaMemcpyHostToDevice));
     NCK(cudaMemcpy(d_filter, fbuf, (size_t)g.filter_width * g.filter_width * sizeof(float), cudaMemcpyHostToDevice));
     if (de_on)
       NCK(cudaMemcpy(d_de, fbuf + (size_t)g.filter_width * g.filter_width,
                      (size_t)(mfi + 1) * 4 * sizeof(float), cudaMemcpyHostToDevice));
     const int shuffle = f3g_opts.shuffle_every > 0 ? f3g_opts.shuffle_every : 1;
-    int e = f3g_launch_iterate(d_passes, d_prefix, ntemporal, total_chunks, S, shuffle, precision, full, mode, threads,
+    int e = f3g_launch_iterate(d_items, d_prefix, ntemporal, total_chunks, shuffle, precision, full, mode, threads,
                                blocks, d_ctr, 0);
     if (e) {
       f3g_set_error("iterate launch failed: %s", cudaGetErrorString((cudaError_t)e));
@@ -315,6 +324,7 @@ done:
   free(fbuf);
   free(passes);
   free(prefix);
+  free(items);
   f3g_genome_free(&cp);
   stats->render_seconds = 0;
   if (rv) fprintf(stderr, "flam3gpu: %s\n", flam3gpu_last_error());

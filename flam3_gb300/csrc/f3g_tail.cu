@@ -154,6 +154,18 @@ extern "C" int f3g_launch_filter_tonemap(const void *acc, int akind, int W, int 
   return (int)cudaGetLastError();
 }
 
+/* The shared-memory limit is raised once, to the largest size a launch asks
+ * for, so that launches inside stream capture make no attribute calls. */
+static volatile int fused_log_attr_done = 0;
+
+extern "C" int f3g_tail_prepare(void) {
+  if (fused_log_attr_done) return 0;
+  cudaError_t e = cudaFuncSetAttribute(k_fused_log_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e != cudaSuccess) return (int)e;
+  fused_log_attr_done = 1;
+  return 0;
+}
+
 extern "C" int f3g_launch_fused_log_filter(const void *buckets, int bkind, int W, int H, double k1, double k2,
                                            int de_offset, int oversample, const float *filter, int fw, int image_w,
                                            int image_h, unsigned char *out, int earlyclip, const F3GTonemap *tp,
@@ -161,8 +173,8 @@ extern "C" int f3g_launch_fused_log_filter(const void *buckets, int bkind, int W
   int sw = FL_TX * oversample + fw - oversample, sh = FL_TY * oversample + fw - oversample;
   size_t smem = (size_t)sw * sh * sizeof(float4) + (size_t)fw * fw * sizeof(float);
   if (smem > 200 * 1024) return -1;
-  cudaError_t e = cudaFuncSetAttribute(k_fused_log_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return (int)e;
+  int e = f3g_tail_prepare();
+  if (e) return e;
   dim3 block(FL_TX, FL_TY), grid((image_w + FL_TX - 1) / FL_TX, (image_h + FL_TY - 1) / FL_TY);
   k_fused_log_filter<<<grid, block, smem, st>>>(buckets, bkind, W, H, (float)k1, (float)k2, de_offset, oversample,
                                                 filter, fw, image_w, image_h, out, earlyclip, *tp);

@@ -74,6 +74,7 @@ typedef struct {
   F3GPass *d_passes; size_t passes_bytes;
   F3GPass *h_passes; size_t h_passes_bytes; /* pinned */
   long long *d_prefix; size_t prefix_bytes; long long *h_prefix; size_t prefix_n;
+  F3GItem *d_items; size_t d_items_bytes; F3GItem *h_items; size_t h_items_n; /* pinned */
   F3GCounters *d_ctr; F3GCounters *h_ctr;
   float *d_filter; size_t filter_bytes;
   float *d_de_w; size_t de_w_bytes;

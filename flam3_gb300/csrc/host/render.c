@@ -15,6 +15,7 @@
  */
 #define _GNU_SOURCE
 #include <math.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -90,6 +91,16 @@ static int ensure_host_passes(f3g_ctx *c, size_t n) {
       return 1;
     }
     c->prefix_n = n + 1;
+  }
+  if (!(c->h_items && c->h_items_n >= n)) {
+    if (c->h_items) cudaFreeHost(c->h_items);
+    c->h_items = NULL;
+    c->h_items_n = 0;
+    if (cudaMallocHost((void **)&c->h_items, n * sizeof(F3GItem)) != cudaSuccess) {
+      f3g_set_error("cudaMallocHost of the work list failed");
+      return 1;
+    }
+    c->h_items_n = n;
   }
   return 0;
 }
@@ -340,6 +351,7 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
   if (ensure_host_passes(c, (size_t)ntemporal)) goto done;
   if (f3g_ensure((void **)&c->d_passes, &c->passes_bytes, (size_t)ntemporal * sizeof(F3GPass))) goto done;
   if (f3g_ensure((void **)&c->d_prefix, &c->prefix_bytes, (size_t)(ntemporal + 1) * sizeof(long long))) goto done;
+  if (f3g_ensure((void **)&c->d_items, &c->d_items_bytes, (size_t)ntemporal * sizeof(F3GItem))) goto done;
   const int precision = f3g_opts.iter_precision == 64 ? 64 : 32;
   double vibrancy = 0.0, gamma = 0.0, background[3] = {0, 0, 0};
   int vib_gam_n = 0;
@@ -432,19 +444,28 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
       if (occ < 1) occ = 1;
       int blocks = f3g_opts.blocks > 0 ? f3g_opts.blocks : c->nsm * occ;
       int S = f3g_chunk_samples(c, batch_samples, threads, blocks, spec->sub_batch_size);
+      unsigned long long *d_counts =
+          (unsigned long long *)((char *)c->d_ctr + offsetof(F3GCounters, badvals));
       for (int ts = 0; ts < ntemporal; ts++) {
         F3GPass *p = &c->h_passes[ts];
+        p->S = S;
+        p->counters = d_counts;
         p->chunk_begin = total_chunks;
         p->nchunks = (p->samples + (long long)threads * S - 1) / ((long long)threads * S);
         total_chunks += p->nchunks;
         c->h_prefix[ts] = p->chunk_begin;
+        c->h_items[ts].pass = c->d_passes + ts;
+        c->h_items[ts].chunk_first = 0;
       }
       c->h_prefix[ntemporal] = total_chunks;
       CK(cudaMemcpyAsync(c->d_passes, c->h_passes, (size_t)ntemporal * sizeof(F3GPass),
                                cudaMemcpyHostToDevice, c->stream));
-      h2d += (double)ntemporal * sizeof(F3GPass) + (double)(ntemporal + 1) * sizeof(long long);
+      h2d += (double)ntemporal * sizeof(F3GPass) + (double)(ntemporal + 1) * sizeof(long long) +
+             (double)ntemporal * sizeof(F3GItem);
       CK(cudaMemcpyAsync(c->d_prefix, c->h_prefix, (size_t)(ntemporal + 1) * sizeof(long long),
                                cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemcpyAsync(c->d_items, c->h_items, (size_t)ntemporal * sizeof(F3GItem), cudaMemcpyHostToDevice,
+                         c->stream));
       int shuffle = f3g_opts.shuffle_every > 0 ? f3g_opts.shuffle_every : 1;
       /* rounds: one launch, or ~10 launches with progress callbacks between */
       int nrounds = spec->progress ? 10 : 1;
@@ -460,7 +481,7 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         h2d += sizeof(F3GCounters);
         d2h += sizeof(F3GCounters);
         CK(cudaEventRecord(c->ev[0], c->stream));
-        int e = f3g_launch_iterate(c->d_passes, c->d_prefix, ntemporal, hi, S, shuffle, precision, full, mode,
+        int e = f3g_launch_iterate(c->d_items, c->d_prefix, ntemporal, hi, shuffle, precision, full, mode,
                                    threads, blocks, c->d_ctr, c->stream);
         launches++;
         if (e) {

@@ -12,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_functions():
     names = set()
-    for h in ("flam3_gpu.h", "flam3_gpu_kernels.h"):
+    for h in sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")):
         txt = open(os.path.join(ROOT, "include", h)).read()
         txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
         for m in re.finditer(r"\b(flam3gpu_\w+)\s*\(", txt):
@@ -29,7 +29,7 @@ def test_library_exports_every_declared_function():
                           check=True).stdout
     exported = {line.split()[-1] for line in syms.splitlines() if " T " in line}
     names = declared_functions()
-    assert len(names) >= 13
+    assert len(names) >= 28
     missing = [n for n in names if n not in exported]
     assert not missing, missing
     lib = render.load()
@@ -53,3 +53,14 @@ def test_options_validation_without_gpu():
     assert lib.flam3gpu_set_options(C.byref(bad)) != 0
     assert lib.flam3gpu_set_options(C.byref(o)) == 0
     assert render.version().startswith("flam3-gb300")
+
+
+def test_service_config_defaults_without_gpu():
+    from flam3_gb300 import service
+
+    c = service.config()
+    assert c.tail_graphs == 1 and c.streams == 2 and c.use_tuning == 1
+    assert c.round_samples == 0 and c.hbm_budget_bytes == 0.0
+    c = service.config(round_samples=-1, streams=3)
+    assert c.round_samples == -1 and c.streams == 3
+
