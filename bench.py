@@ -18,6 +18,22 @@ genome comes from a seeded generator (flam3_gb300.genome.config1_genome).
          write per plotted sample) and for the DE/filter/tonemap tail
          (histogram read + image write)
 
+The same line carries the batched and served legs of the metric
+("renders/s and p50/p99 latency, served vs plain"):
+
+  batched_animation  config 2: two 5-xform genomes interpolated over 120
+         frames of 1280x720 q500, 100 temporal samples, DE r7; the plain
+         drop-in frame after frame vs flam3gpu_render_batch (one persistent
+         launch over all frames and temporal samples, graph-captured tails)
+  batched_mixed      config 3: 256 mixed-size jobs, plain one at a time vs
+         one batch
+  served             config 4: a Poisson trace (95% config-3 jobs, 5%
+         3840x2160 q1000 ss2 DE11); renders/s at saturation and p50/p95/p99
+         latency at one arrival rate, plain (one request at a time) vs the
+         render service (continuous batching); plus the mean absolute
+         difference of the two arms' images, and both arms' error against
+         16x-quality renders of a few requests
+
 `--impl reference` times the CPU implementation of the same path on the
 host cores (the oracle build of the reference algorithm, all host threads)
 on a bounded sample of the same workload (quality reduced), same metric.
@@ -239,7 +255,139 @@ def run_gpu(args):
         "clocks": clk.summary(),
         "cpu_baseline": cb,
     }
+    if world == 1 and args.legs:
+        line.update(run_legs(args))
     print(json.dumps(line))
+
+
+def pct(xs, q):
+    import numpy as np
+
+    return float(np.percentile(np.asarray(xs, dtype=float), q)) if xs else None
+
+
+def mae(a, b):
+    import numpy as np
+
+    return float(np.mean(np.abs(a.astype(np.float64) - b.astype(np.float64))))
+
+
+def leg_batched(name, make_frames, note):
+    """plain drop-in one frame at a time vs one flam3gpu_render_batch call"""
+    import torch
+    from flam3_gb300 import render, service
+
+    frames = make_frames("p")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_imgs, iters = [], 0
+    for F in frames:
+        img, st = render.render(F)
+        plain_imgs.append(img)
+        iters += st.num_iters
+    t_plain = time.perf_counter() - t0
+    frames = make_frames("p")  # same seeds: same samples, up to atomic order
+    t0 = time.perf_counter()
+    res = service.render_batch(frames)
+    t_batch = time.perf_counter() - t0
+    n = len(frames)
+    diff = max(mae(a, b[0]) for a, b in zip(plain_imgs, res))
+    return {"workload": note, "renders": n, "iterations": iters,
+            "plain_renders_per_s": n / t_plain, "batched_renders_per_s": n / t_batch,
+            "speedup": t_plain / t_batch, "plain_s": t_plain, "batched_s": t_batch,
+            "plain_giter_s": iters / t_plain / 1e9, "batched_giter_s": iters / t_batch / 1e9,
+            "max_mae_batched_vs_plain": diff}
+
+
+def leg_served(nreq, seed=4, ref_check=3):
+    """config 4 trace: saturation throughput and latency at one arrival rate"""
+    import numpy as np
+    from flam3_gb300 import genome as gm, render, service
+
+    def trace(rate):
+        tr = gm.config4_trace(seed=seed, nrequests=nreq, rate_hz=rate)
+        return [(t, gm.Frame(G, bits=b, seed="srv-%d" % i)) for i, (t, G, b) in enumerate(tr)]
+
+    # saturation: every request queued at t=0
+    reqs = trace(1.0)
+    t0 = time.perf_counter()
+    plain_imgs = []
+    for _, F in reqs:
+        plain_imgs.append(render.render(F)[0])
+    t_plain = time.perf_counter() - t0
+    reqs = trace(1.0)
+    with service.Service() as svc:
+        t0 = time.perf_counter()
+        tk = [svc.submit(F) for _, F in reqs]
+        served_imgs = [svc.wait(t)[0] for t in tk]
+        t_served = time.perf_counter() - t0
+        cnt = svc.counters()
+    cap_plain = nreq / t_plain
+    # latency at 70% of the plain path's capacity (a load the plain path sustains)
+    rate = 0.7 * cap_plain
+    reqs = trace(rate)
+    lat_plain = []
+    start = time.perf_counter()
+    for t_arr, F in reqs:
+        now = time.perf_counter() - start
+        if now < t_arr:
+            time.sleep(t_arr - now)
+        render.render(F)
+        lat_plain.append((time.perf_counter() - start) - t_arr)
+    reqs = trace(rate)
+    lat_served = []
+    with service.Service() as svc:
+        tickets = []
+        start = time.perf_counter()
+        for t_arr, F in reqs:
+            now = time.perf_counter() - start
+            if now < t_arr:
+                time.sleep(t_arr - now)
+            tickets.append(svc.submit(F))
+        for t in tickets:
+            _, _, tm = svc.wait(t)  # tm[2]: submit -> done, measured by the service
+            lat_served.append(tm[2] / 1e3)
+    diffs = [mae(a, b) for a, b in zip(plain_imgs, served_imgs)]
+    # error against 16x-quality renders for a few small requests
+    errs = []
+    small = [i for i, (_, F) in enumerate(trace(1.0)) if F.width * F.height <= 512 * 512][:ref_check]
+    for i in small:
+        _, F = trace(1.0)[i]
+        G = F.genomes[0]
+        G.g.sample_density *= 16
+        hq = render.render(gm.Frame(G, bits=64, seed="hq-%d" % i))[0]
+        errs.append({"request": i, "mae_plain": mae(plain_imgs[i], hq) / 255.0,
+                     "mae_served": mae(served_imgs[i], hq) / 255.0})
+    q = lambda xs: {"p50": 1e3 * pct(xs, 50), "p95": 1e3 * pct(xs, 95), "p99": 1e3 * pct(xs, 99)}
+    return {"workload": "config4 trace: %d requests, 95%% config-3 jobs, 5%% 3840x2160 q1000 ss2 DE11" % nreq,
+            "plain_renders_per_s": cap_plain, "served_renders_per_s": nreq / t_served,
+            "speedup": t_plain / t_served, "rate_hz": rate,
+            "latency_ms_plain": q(lat_plain), "latency_ms_served": q(lat_served),
+            "mean_mae_served_vs_plain": float(np.mean(diffs)), "max_mae_served_vs_plain": float(np.max(diffs)),
+            "error_vs_16x": errs, "service_rounds": cnt["rounds"], "service_launches": cnt["launches"],
+            "peak_device_gb": cnt["peak_device_bytes"] / 1e9}
+
+
+def run_legs(args):
+    from flam3_gb300 import genome as gm
+
+    out = {}
+    if "c2" in args.legs:
+        def c2(tag):
+            gs = gm.config2_genomes(2)
+            return [gm.Frame(gs, bits=33, seed="c2-%s-%d" % (tag, i), time=float(i)) for i in range(args.c2_frames)]
+
+        out["batched_animation"] = leg_batched("c2", c2, "config2: %d frames 1280x720 q500 100 temporal samples DE7"
+                                               % args.c2_frames)
+    if "c3" in args.legs:
+        def c3(tag):
+            return [gm.Frame(G, bits=b, seed="c3-%s-%d" % (tag, i))
+                    for i, (G, b) in enumerate(gm.config3_jobs(3, njobs=args.c3_jobs))]
+
+        out["batched_mixed"] = leg_batched("c3", c3, "config3: %d mixed jobs" % args.c3_jobs)
+    if "c4" in args.legs:
+        out["served"] = leg_served(args.c4_requests)
+    return out
 
 
 def main():
@@ -249,6 +397,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--legs", default="c2,c3,c4", help="batched/served legs to add (c2,c3,c4; empty: none)")
+    ap.add_argument("--c2-frames", type=int, default=120)
+    ap.add_argument("--c3-jobs", type=int, default=256)
+    ap.add_argument("--c4-requests", type=int, default=64)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
