@@ -281,22 +281,32 @@ def leg_batched(name, make_frames, note):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     plain_imgs, iters = [], 0
+    dev = {"iterate_ms": 0.0, "de_ms": 0.0, "tail_ms": 0.0}
     for F in frames:
         img, st = render.render(F)
         plain_imgs.append(img)
         iters += st.num_iters
+        t = render.last_timings()
+        for k in dev:
+            dev[k] += t[k]
     t_plain = time.perf_counter() - t0
     frames = make_frames("p")  # same seeds: same samples, up to atomic order
-    t0 = time.perf_counter()
-    res = service.render_batch(frames)
-    t_batch = time.perf_counter() - t0
+    with service.Service(round_samples=-1) as svc:  # one persistent launch per round over all frames
+        t0 = time.perf_counter()
+        tk = svc.submit_many(frames)
+        res = [svc.wait(t)[:2] for t in tk]
+        t_batch = time.perf_counter() - t0
+        cnt = svc.counters()
     n = len(frames)
     diff = max(mae(a, b[0]) for a, b in zip(plain_imgs, res))
     return {"workload": note, "renders": n, "iterations": iters,
             "plain_renders_per_s": n / t_plain, "batched_renders_per_s": n / t_batch,
             "speedup": t_plain / t_batch, "plain_s": t_plain, "batched_s": t_batch,
             "plain_giter_s": iters / t_plain / 1e9, "batched_giter_s": iters / t_batch / 1e9,
-            "max_mae_batched_vs_plain": diff}
+            "plain_device_s": {k.replace("_ms", "_s"): v / 1e3 for k, v in dev.items()},
+            "max_mae_batched_vs_plain": diff, "service": {k: cnt[k] for k in (
+                "rounds", "launches", "tail_graphs", "graphs_instantiated", "peak_device_bytes", "host_admit_s",
+                "host_round_s", "host_tail_s", "host_complete_s", "host_wait_s", "gpu_iterate_s", "gpu_tail_s")}}
 
 
 def leg_served(nreq, seed=4, ref_check=3):
@@ -312,8 +322,12 @@ def leg_served(nreq, seed=4, ref_check=3):
     reqs = trace(1.0)
     t0 = time.perf_counter()
     plain_imgs = []
+    dev = {"iterate_ms": 0.0, "de_ms": 0.0, "tail_ms": 0.0}
     for _, F in reqs:
         plain_imgs.append(render.render(F)[0])
+        t = render.last_timings()
+        for k in dev:
+            dev[k] += t[k]
     t_plain = time.perf_counter() - t0
     reqs = trace(1.0)
     with service.Service() as svc:
@@ -361,11 +375,13 @@ def leg_served(nreq, seed=4, ref_check=3):
     q = lambda xs: {"p50": 1e3 * pct(xs, 50), "p95": 1e3 * pct(xs, 95), "p99": 1e3 * pct(xs, 99)}
     return {"workload": "config4 trace: %d requests, 95%% config-3 jobs, 5%% 3840x2160 q1000 ss2 DE11" % nreq,
             "plain_renders_per_s": cap_plain, "served_renders_per_s": nreq / t_served,
+            "plain_device_s": {k.replace("_ms", "_s"): v / 1e3 for k, v in dev.items()},
             "speedup": t_plain / t_served, "rate_hz": rate,
             "latency_ms_plain": q(lat_plain), "latency_ms_served": q(lat_served),
             "mean_mae_served_vs_plain": float(np.mean(diffs)), "max_mae_served_vs_plain": float(np.max(diffs)),
-            "error_vs_16x": errs, "service_rounds": cnt["rounds"], "service_launches": cnt["launches"],
-            "peak_device_gb": cnt["peak_device_bytes"] / 1e9}
+            "error_vs_16x": errs, "service": {k: cnt[k] for k in (
+                "rounds", "launches", "tail_graphs", "graphs_instantiated", "peak_device_bytes", "host_admit_s",
+                "host_round_s", "host_tail_s", "host_complete_s", "host_wait_s", "gpu_iterate_s", "gpu_tail_s")}}
 
 
 def run_legs(args):

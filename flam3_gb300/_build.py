@@ -1,7 +1,12 @@
 """Builds libflam3gpu.so in-tree: nvcc for the CUDA kernels (sm_103a only),
 gcc for the C host driver, translation units compiled in parallel.
 
-Usage: python -m flam3_gb300._build [--force]
+Usage: python -m flam3_gb300._build [--force] [--define NAME ...] [--out PATH]
+
+--define adds a preprocessor macro to the CUDA sources (for example
+F3G_FAST_MATH); --out writes the library elsewhere (its objects go to a
+sibling build directory), so variants can sit beside the default build and
+be loaded with FLAM3GPU_LIB=PATH.
 """
 import concurrent.futures as cf
 import os
@@ -36,8 +41,8 @@ def headers():
     return out
 
 
-def _obj(src):
-    return os.path.join(BUILD, os.path.basename(src) + ".o")
+def _obj(src, bdir=BUILD):
+    return os.path.join(bdir, os.path.basename(src) + ".o")
 
 
 def _stale(obj, deps):
@@ -54,30 +59,33 @@ def _compile(cmd):
     return r.stderr
 
 
-def build(force=False, verbose=False):
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, defines=(), out=None):
+    lib = out or LIB
+    bdir = BUILD if out is None else os.path.splitext(lib)[0] + "_build"
+    os.makedirs(bdir, exist_ok=True)
     cu, c = sources()
     hdrs = headers()
+    dflags = ["-D" + d for d in defines]
     jobs = []
     for s in cu:
-        o = _obj(s)
+        o = _obj(s, bdir)
         if force or _stale(o, [s] + hdrs):
-            jobs.append([NVCC] + NVCC_FLAGS + ["-c", s, "-o", o])
+            jobs.append([NVCC] + NVCC_FLAGS + dflags + ["-c", s, "-o", o])
     for s in c:
-        o = _obj(s)
+        o = _obj(s, bdir)
         if force or _stale(o, [s] + hdrs):
-            jobs.append(["gcc"] + CC_FLAGS + ["-c", s, "-o", o])
+            jobs.append(["gcc"] + CC_FLAGS + dflags + ["-c", s, "-o", o])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
             for msg in ex.map(_compile, jobs):
                 if verbose and msg:
                     print(msg)
-    objs = [_obj(s) for s in cu + c]
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB + ".tmp"
+    objs = [_obj(s, bdir) for s in cu + c]
+    if force or jobs or _stale(lib, objs):
+        tmp = lib + ".tmp"
         _compile([NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread", "-lm"])
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 def build_oracle(with_reference=None):
@@ -94,4 +102,7 @@ def build_oracle(with_reference=None):
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))
+    argv = sys.argv[1:]
+    defs = [argv[i + 1] for i, a in enumerate(argv) if a == "--define"]
+    outp = [argv[i + 1] for i, a in enumerate(argv) if a == "--out"]
+    print(build(force="--force" in argv, verbose=True, defines=defs, out=os.path.abspath(outp[0]) if outp else None))

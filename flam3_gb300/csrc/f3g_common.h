@@ -14,6 +14,7 @@
 #ifndef F3G_COMMON_H
 #define F3G_COMMON_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #define F3G_MAX_XFORMS 32      /* standard + final xforms of one genome */
@@ -100,7 +101,6 @@ typedef struct {
    * random 14-bit value v is the number of entries in brk[r] that are <= v. */
   uint16_t nbrk[F3G_MAX_XFORMS + 1];
   uint16_t brk[F3G_MAX_XFORMS + 1][F3G_MAX_XFORMS];
-  F3GXform xf[F3G_MAX_XFORMS];
   uint8_t var_id[F3G_MAX_VARLIST];
   double var_w[F3G_MAX_VARLIST];
   /* --- colour -------------------------------------------------------- */
@@ -120,7 +120,12 @@ typedef struct {
   int bucket_kind;
   int S;                    /* samples per thread per chunk: a chunk is blockDim*S samples */
   unsigned long long *counters; /* [0] bad values, [1] samples plotted (device) */
+  /* --- xforms last: a pass is uploaded up to its last used xform ------ */
+  F3GXform xf[F3G_MAX_XFORMS];
 } F3GPass;
+
+/* bytes of a pass that hold data when its genome has nx xforms */
+#define F3G_PASS_BYTES(nx) (offsetof(F3GPass, xf) + (size_t)(nx) * sizeof(F3GXform))
 
 /* One entry of an iterate launch's work list: chunks [chunk_first,
  * chunk_first + n) of a pass, where n is the entry's span in the launch's

@@ -95,24 +95,48 @@ template <> __device__ __forceinline__ double u11<double>(uint32_t w) {
 /* ---------------------------------------------------------------------
  * precision-generic math
  * ------------------------------------------------------------------- */
+/* FP32 iteration uses the hardware approximations of sin, cos, exp, log and
+ * pow (the chain is chaotic; the FP32 bound of the apply_xform tests covers
+ * them, and whole-render error against a 16x-quality render is unchanged);
+ * build with F3G_ACCURATE_MATH for the libm-accurate FP32 functions.  FP64
+ * always uses the accurate functions. */
+#if !defined(F3G_ACCURATE_MATH) && !defined(F3G_FAST_MATH)
+#define F3G_FAST_MATH
+#endif
+#ifdef F3G_FAST_MATH
+__device__ __forceinline__ float m_sin(float x) { return __sinf(x); }
+__device__ __forceinline__ float m_cos(float x) { return __cosf(x); }
+__device__ __forceinline__ void m_sincos(float x, float *s, float *c) { __sincosf(x, s, c); }
+__device__ __forceinline__ float m_exp(float x) { return __expf(x); }
+__device__ __forceinline__ float m_log(float x) { return __logf(x); }
+__device__ __forceinline__ float m_pow(float x, float y) { return __powf(x, y); }
+#else
 __device__ __forceinline__ float m_sin(float x) { return sinf(x); }
-__device__ __forceinline__ double m_sin(double x) { return sin(x); }
 __device__ __forceinline__ float m_cos(float x) { return cosf(x); }
-__device__ __forceinline__ double m_cos(double x) { return cos(x); }
 __device__ __forceinline__ void m_sincos(float x, float *s, float *c) { sincosf(x, s, c); }
+__device__ __forceinline__ float m_exp(float x) { return expf(x); }
+__device__ __forceinline__ float m_log(float x) { return logf(x); }
+__device__ __forceinline__ float m_pow(float x, float y) { return powf(x, y); }
+#endif
+/* quotient: with fast math FP32 uses the approximate divide (2 ulp) */
+#ifdef F3G_FAST_MATH
+__device__ __forceinline__ float m_div(float a, float b) { return __fdividef(a, b); }
+#else
+__device__ __forceinline__ float m_div(float a, float b) { return a / b; }
+#endif
+__device__ __forceinline__ double m_div(double a, double b) { return a / b; }
+__device__ __forceinline__ double m_sin(double x) { return sin(x); }
+__device__ __forceinline__ double m_cos(double x) { return cos(x); }
 __device__ __forceinline__ void m_sincos(double x, double *s, double *c) { sincos(x, s, c); }
+__device__ __forceinline__ double m_exp(double x) { return exp(x); }
+__device__ __forceinline__ double m_log(double x) { return log(x); }
+__device__ __forceinline__ double m_pow(double x, double y) { return pow(x, y); }
 __device__ __forceinline__ float m_tan(float x) { return tanf(x); }
 __device__ __forceinline__ double m_tan(double x) { return tan(x); }
 __device__ __forceinline__ float m_atan2(float y, float x) { return atan2f(y, x); }
 __device__ __forceinline__ double m_atan2(double y, double x) { return atan2(y, x); }
 __device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
-__device__ __forceinline__ float m_pow(float x, float y) { return powf(x, y); }
-__device__ __forceinline__ double m_pow(double x, double y) { return pow(x, y); }
-__device__ __forceinline__ float m_exp(float x) { return expf(x); }
-__device__ __forceinline__ double m_exp(double x) { return exp(x); }
-__device__ __forceinline__ float m_log(float x) { return logf(x); }
-__device__ __forceinline__ double m_log(double x) { return log(x); }
 __device__ __forceinline__ float m_log10(float x) { return log10f(x); }
 __device__ __forceinline__ double m_log10(double x) { return log10(x); }
 __device__ __forceinline__ float m_sinh(float x) { return sinhf(x); }
@@ -162,14 +186,14 @@ __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R>
   switch (v) {
     case 0: f.p0 += w * f.tx; f.p1 += w * f.ty; break;
     case 1: f.p0 += w * m_sin(f.tx); f.p1 += w * m_sin(f.ty); break;
-    case 2: { R r2 = w / (f.sumsq + EPS_R); f.p0 += r2 * f.tx; f.p1 += r2 * f.ty; } break;
+    case 2: { R r2 = m_div(w, f.sumsq + EPS_R); f.p0 += r2 * f.tx; f.p1 += r2 * f.ty; } break;
     case 3: {
       R c1, c2; m_sincos(f.sumsq, &c1, &c2);
       R nx = c1 * f.tx - c2 * f.ty, ny = c2 * f.tx + c1 * f.ty;
       f.p0 += w * nx; f.p1 += w * ny;
     } break;
     case 4: {
-      R r = w / (f.sqrtv + EPS_R);
+      R r = m_div(w, f.sqrtv + EPS_R);
       f.p0 += (f.tx - f.ty) * (f.tx + f.ty) * r; f.p1 += (R)2.0 * f.tx * f.ty * r;
     } break;
     case 5: f.p0 += w * (f.atan_xy * ONE_PI_R); f.p1 += w * (f.sqrtv - (R)1.0); break;
@@ -186,10 +210,10 @@ __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R>
       f.p0 += w * sr * a; f.p1 += w * cr * a;
     } break;
     case 9: {
-      R r = f.sqrtv + EPS_R, r1 = w / r, sr, cr; m_sincos(r, &sr, &cr);
+      R r = f.sqrtv + EPS_R, r1 = m_div(w, r), sr, cr; m_sincos(r, &sr, &cr);
       f.p0 += r1 * (f.cosa + sr); f.p1 += r1 * (f.sina - cr);
     } break;
-    case 10: { R r = f.sqrtv + EPS_R; f.p0 += w * f.sina / r; f.p1 += w * f.cosa * r; } break;
+    case 10: { R r = f.sqrtv + EPS_R; f.p0 += m_div(w * f.sina, r); f.p1 += w * f.cosa * r; } break;
     case 11: {
       R sr, cr; m_sincos(f.sqrtv, &sr, &cr);
       f.p0 += w * f.sina * cr; f.p1 += w * f.cosa * sr;
@@ -216,7 +240,7 @@ __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R>
       R ny = f.ty + x.c[3] * m_sin(f.tx * P(waves_dy2));
       f.p0 += w * nx; f.p1 += w * ny;
     } break;
-    case 16: { R r = (R)2 * w / (f.sqrtv + (R)1); f.p0 += r * f.ty; f.p1 += r * f.tx; } break;
+    case 16: { R r = m_div((R)2 * w, f.sqrtv + (R)1); f.p0 += r * f.ty; f.p1 += r * f.tx; } break;
     case 17: {
       R dx = m_tan((R)3 * f.ty), dy = m_tan((R)3 * f.tx);
       R nx = f.tx + x.c[4] * m_sin(dx), ny = f.ty + x.c[5] * m_sin(dy);
@@ -757,8 +781,8 @@ __device__ __forceinline__ bool apply_xform(const XfS<R> &x, const uint8_t *var_
   f.atan_xy = f.sina = f.cosa = f.atan_yx = (R)0;
   if (x.flags & F3G_F_ATAN_XY) f.atan_xy = m_atan2(f.tx, f.ty);
   if (x.flags & F3G_F_ANGLES) {
-    f.sina = f.tx / f.sqrtv;
-    f.cosa = f.ty / f.sqrtv;
+    f.sina = m_div(f.tx, f.sqrtv);
+    f.cosa = m_div(f.ty, f.sqrtv);
   }
   if (x.flags & F3G_F_ATAN_YX) f.atan_yx = m_atan2(f.ty, f.tx);
   f.p0 = (R)0;

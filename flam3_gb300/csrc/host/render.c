@@ -458,9 +458,13 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         c->h_items[ts].chunk_first = 0;
       }
       c->h_prefix[ntemporal] = total_chunks;
-      CK(cudaMemcpyAsync(c->d_passes, c->h_passes, (size_t)ntemporal * sizeof(F3GPass),
-                               cudaMemcpyHostToDevice, c->stream));
-      h2d += (double)ntemporal * sizeof(F3GPass) + (double)(ntemporal + 1) * sizeof(long long) +
+      int nxmax = 0;
+      for (int ts = 0; ts < ntemporal; ts++)
+        if (c->h_passes[ts].num_xforms > nxmax) nxmax = c->h_passes[ts].num_xforms;
+      const size_t pass_bytes = F3G_PASS_BYTES(nxmax);
+      CK(cudaMemcpy2DAsync(c->d_passes, sizeof(F3GPass), c->h_passes, sizeof(F3GPass), pass_bytes,
+                           (size_t)ntemporal, cudaMemcpyHostToDevice, c->stream));
+      h2d += (double)ntemporal * pass_bytes + (double)(ntemporal + 1) * sizeof(long long) +
              (double)ntemporal * sizeof(F3GItem);
       CK(cudaMemcpyAsync(c->d_prefix, c->h_prefix, (size_t)(ntemporal + 1) * sizeof(long long),
                                cudaMemcpyHostToDevice, c->stream));

@@ -104,12 +104,12 @@ typedef struct {
   long long *h_prefix, *d_prefix;
   size_t cap; /* items */
   F3GCounters *d_ctr; /* one per class */
-  cudaEvent_t ev;
+  cudaEvent_t ev, t0, t1; /* completion; timing of the round's launches */
   int in_use;
 } round_buf;
 
 typedef struct {
-  cudaEvent_t ev;
+  cudaEvent_t ev, t0; /* completion (timed) and start of the slot's tail work */
   int in_use, njobs;
   f3g_job **jobs;
   int cap;
@@ -146,19 +146,22 @@ struct flam3gpu_service {
   unsigned long long tail_no;
   graph_entry graphs[NGRAPH];
   unsigned long long graph_clock;
-  /* pinned host buffers kept for reuse (freeing pinned memory synchronizes
-   * the device); size classes are powers of two from 64 KiB */
-  struct pin_buf {
-    void *p;
-    size_t cap;
-    struct pin_buf *next;
-  } *pin_free[40];
-  pthread_mutex_t pin_mu;
-  int paused; /* submissions held back until released (render_batch) */
   /* counters */
   double c_done, c_failed, c_rounds, c_launches, c_graphs, c_inst, c_plotted, c_h2d, c_d2h;
+  double h_admit, h_round, h_tail, h_done, h_wait; /* service-thread seconds by activity */
+  double g_iter, g_tail;                           /* device seconds of iterate rounds and of tails */
   double t_first_admit, t_last_done;
 };
+
+/* Pinned host staging buffers, kept for reuse by every service of the
+ * process (allocating and freeing pinned memory is slow and freeing it
+ * synchronizes the device); size classes are powers of two from 64 KiB. */
+struct pin_buf {
+  void *p;
+  struct pin_buf *next;
+};
+static struct pin_buf *g_pin_free[40];
+static pthread_mutex_t g_pin_mu = PTHREAD_MUTEX_INITIALIZER;
 
 static int pin_class(size_t n) {
   int c = 16;
@@ -166,12 +169,12 @@ static int pin_class(size_t n) {
   return c;
 }
 
-static void *pin_get(flam3gpu_service *s, size_t n) {
+static void *pin_get(size_t n) {
   const int c = pin_class(n);
-  pthread_mutex_lock(&s->pin_mu);
-  struct pin_buf *b = s->pin_free[c];
-  if (b) s->pin_free[c] = b->next;
-  pthread_mutex_unlock(&s->pin_mu);
+  pthread_mutex_lock(&g_pin_mu);
+  struct pin_buf *b = g_pin_free[c];
+  if (b) g_pin_free[c] = b->next;
+  pthread_mutex_unlock(&g_pin_mu);
   if (b) {
     void *p = b->p;
     free(b);
@@ -182,17 +185,16 @@ static void *pin_get(flam3gpu_service *s, size_t n) {
   return p;
 }
 
-static void pin_put(flam3gpu_service *s, void *p, size_t n) {
+static void pin_put(void *p, size_t n) {
   if (!p) return;
   struct pin_buf *b = (struct pin_buf *)malloc(sizeof(*b));
   if (!b) return; /* leaked rather than freed mid-flight */
   const int c = pin_class(n);
   b->p = p;
-  b->cap = (size_t)1 << c;
-  pthread_mutex_lock(&s->pin_mu);
-  b->next = s->pin_free[c];
-  s->pin_free[c] = b;
-  pthread_mutex_unlock(&s->pin_mu);
+  pthread_mutex_lock(&g_pin_mu);
+  b->next = g_pin_free[c];
+  g_pin_free[c] = b;
+  pthread_mutex_unlock(&g_pin_mu);
 }
 
 static double now_s(void) {
@@ -574,9 +576,11 @@ flam3gpu_service *flam3gpu_service_create(const flam3gpu_service_config *cfg_in)
          cudaEventCreateWithFlags(&s->ev_join[k], cudaEventDisableTiming) == cudaSuccess;
   for (int k = 0; ok && k < NRB; k++)
     ok = cudaEventCreateWithFlags(&s->rb[k].ev, cudaEventDisableTiming | cudaEventBlockingSync) == cudaSuccess &&
+         cudaEventCreate(&s->rb[k].t0) == cudaSuccess && cudaEventCreate(&s->rb[k].t1) == cudaSuccess &&
          cudaMalloc((void **)&s->rb[k].d_ctr, NCLASS * sizeof(F3GCounters)) == cudaSuccess;
   for (int k = 0; ok && k < NTAIL; k++)
-    ok = cudaEventCreateWithFlags(&s->ts[k].ev, cudaEventDisableTiming | cudaEventBlockingSync) == cudaSuccess;
+    ok = cudaEventCreateWithFlags(&s->ts[k].ev, cudaEventBlockingSync) == cudaSuccess &&
+         cudaEventCreate(&s->ts[k].t0) == cudaSuccess;
   if (ok) ok = cudaDeviceGetDefaultMemPool(&s->pool, s->device) == cudaSuccess;
   if (ok) {
     uint64_t thr = ~(uint64_t)0;
@@ -594,7 +598,6 @@ flam3gpu_service *flam3gpu_service_create(const flam3gpu_service_config *cfg_in)
   if (want > 0.9 * (double)freeb) want = 0.9 * (double)freeb;
   s->budget = (size_t)want;
   pthread_mutex_init(&s->mu, NULL);
-  pthread_mutex_init(&s->pin_mu, NULL);
   pthread_cond_init(&s->cv_work, NULL);
   pthread_cond_init(&s->cv_done, NULL);
   if (pthread_create(&s->thread, NULL, service_main, s) != 0) {
@@ -692,8 +695,12 @@ static int admit_job(flam3gpu_service *s, f3g_job *j) {
       p->count = j->bp[b].use_count ? j->d_count : NULL;
       p->counters = j->d_counts;
     }
-  int ok = cudaMemcpyAsync(j->d_passes, j->h_passes, (size_t)npass * sizeof(F3GPass), cudaMemcpyHostToDevice,
-                           s->s_up) == cudaSuccess;
+  int nxmax = 0;
+  for (int i = 0; i < npass; i++)
+    if (j->h_passes[i].num_xforms > nxmax) nxmax = j->h_passes[i].num_xforms;
+  const size_t pass_bytes = F3G_PASS_BYTES(nxmax);
+  int ok = cudaMemcpy2DAsync(j->d_passes, sizeof(F3GPass), j->h_passes, sizeof(F3GPass), pass_bytes, (size_t)npass,
+                             cudaMemcpyHostToDevice, s->s_up) == cudaSuccess;
   ok = ok && cudaMemcpyAsync(j->d_filter, j->h_filter, (size_t)j->g.filter_width * j->g.filter_width * sizeof(float),
                              cudaMemcpyHostToDevice, s->s_up) == cudaSuccess;
   if (j->nkinfo)
@@ -704,7 +711,7 @@ static int admit_job(flam3gpu_service *s, f3g_job *j) {
   if (j->need_acc) ok = ok && cudaMemsetAsync(j->d_acc, 0, (size_t)j->nb * j->bsz, s->s_up) == cudaSuccess;
   ok = ok && cudaMemsetAsync(j->d_counts, 0, 2 * sizeof(unsigned long long), s->s_up) == cudaSuccess;
   if (ok) {
-    j->h_out = (unsigned char *)pin_get(s, align256(j->out_bytes) + 2 * sizeof(unsigned long long));
+    j->h_out = (unsigned char *)pin_get(align256(j->out_bytes) + 2 * sizeof(unsigned long long));
     if (!j->h_out) ok = 0;
   }
   if (ok) j->h_counts = (unsigned long long *)(j->h_out + align256(j->out_bytes));
@@ -716,7 +723,7 @@ static int admit_job(flam3gpu_service *s, f3g_job *j) {
     cudaEventDestroy(ev);
   } else
     ok = 0;
-  s->c_h2d += (double)npass * sizeof(F3GPass) + (double)j->g.filter_width * j->g.filter_width * 4 + j->nkinfo * 4.0;
+  s->c_h2d += (double)npass * pass_bytes + (double)j->g.filter_width * j->g.filter_width * 4 + j->nkinfo * 4.0;
   if (!ok) {
     snprintf(j->err, sizeof(j->err), "device setup failed: %s", cudaGetErrorString(cudaGetLastError()));
     return 1;
@@ -735,7 +742,7 @@ static void release_job_device(flam3gpu_service *s, f3g_job *j) {
     s->used -= j->dev_bytes;
   }
   if (j->h_out) {
-    pin_put(s, j->h_out, align256(j->out_bytes) + 2 * sizeof(unsigned long long));
+    pin_put(j->h_out, align256(j->out_bytes) + 2 * sizeof(unsigned long long));
     j->h_out = NULL;
     j->h_counts = NULL;
   }
@@ -866,7 +873,16 @@ static cudaGraphExec_t graph_for(flam3gpu_service *s, cudaGraph_t graph, const c
 static void finish_slot(flam3gpu_service *s, tail_slot *t);
 
 /* tails of the jobs whose current batch finished in the round just issued */
+static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n);
 static void enqueue_tails(flam3gpu_service *s, f3g_job **jobs, int n) {
+  const double t0 = now_s();
+  enqueue_tails_impl(s, jobs, n);
+  const double dt = now_s() - t0;
+  s->h_tail += dt;
+  s->h_round -= dt; /* reported apart from round building */
+}
+
+static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n) {
   tail_slot *t = &s->ts[s->tail_no % NTAIL];
   if (t->in_use) {
     cudaEventSynchronize(t->ev);
@@ -885,6 +901,7 @@ static void enqueue_tails(flam3gpu_service *s, f3g_job **jobs, int n) {
     t->cap = n;
   }
   for (int k = 0; k < s->cfg.streams; k++) cudaStreamWaitEvent(s->s_tail, s->ev_last[k], 0);
+  cudaEventRecord(t->t0, s->s_tail);
   int err = 0;
   if (s->cfg.tail_graphs) {
     char sig[512];
@@ -941,7 +958,10 @@ static void enqueue_tails(flam3gpu_service *s, f3g_job **jobs, int n) {
   s->tail_no++;
 }
 
-static void complete_job(flam3gpu_service *s, f3g_job *j) {
+/* copies a finished job's staged image to the caller's buffer (rows
+ * interleaved for fields) and returns the staging buffer */
+static void copy_out(f3g_job *j) {
+  if (!j->h_out) return;
   const f3g_geom *g = &j->g;
   const size_t row = (size_t)g->image_width * j->nchan * j->spec.bytes_per_channel;
   unsigned char *dst = (unsigned char *)j->out;
@@ -950,10 +970,21 @@ static void complete_job(flam3gpu_service *s, f3g_job *j) {
   if (dpitch == row) memcpy(dst, j->h_out, row * g->image_height);
   else
     for (int y = 0; y < g->image_height; y++) memcpy(dst + (size_t)y * dpitch, j->h_out + (size_t)y * row, row);
+  pin_put(j->h_out, align256(j->out_bytes) + 2 * sizeof(unsigned long long));
+  j->h_out = NULL;
+  j->h_counts = NULL;
+}
+
+/* the job's tail has run: release its device memory and publish it; the
+ * waiter copies the image out (off the service thread) */
+static void complete_job(flam3gpu_service *s, f3g_job *j) {
   j->stats.badvals = (double)j->h_counts[0];
   s->c_plotted += (double)j->h_counts[1];
   j->stats.render_seconds = (int)(now_s() - j->t_submit);
+  unsigned char *keep = j->h_out;
+  j->h_out = NULL; /* release_job_device leaves the staging buffer to the waiter */
   release_job_device(s, j);
+  j->h_out = keep;
   remove_active(s, j);
   job_free_plan(j);
   pthread_mutex_lock(&s->mu);
@@ -967,6 +998,8 @@ static void complete_job(flam3gpu_service *s, f3g_job *j) {
 }
 
 static void finish_slot(flam3gpu_service *s, tail_slot *t) {
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, t->t0, t->ev) == cudaSuccess) s->g_tail += ms * 1e-3;
   for (int i = 0; i < t->njobs; i++) {
     f3g_job *j = t->jobs[i];
     if (j->batch == j->nbatches - 1) complete_job(s, j);
@@ -1030,6 +1063,8 @@ typedef struct {
   long long span;
   int cls;
 } tmp_item;
+
+static void round_done(flam3gpu_service *s, round_buf *r);
 
 /* one iterate round over the admitted jobs; returns 1 if a round was issued */
 static int issue_round(flam3gpu_service *s) {
@@ -1114,7 +1149,7 @@ static int issue_round(flam3gpu_service *s) {
   round_buf *r = &s->rb[rno % NRB];
   if (r->in_use) {
     cudaEventSynchronize(r->ev);
-    r->in_use = 0;
+    round_done(s, r);
   }
   if (!ti || ensure_round_cap(r, nit + 1)) {
     free(ti);
@@ -1156,6 +1191,7 @@ static int issue_round(flam3gpu_service *s) {
   const int shuffle = f3g_opts.shuffle_every > 0 ? f3g_opts.shuffle_every : 1;
   const int threads = f3g_opts.threads_per_block > 0 ? f3g_opts.threads_per_block : 256;
   const int precision = f3g_opts.iter_precision == 64 ? 64 : 32;
+  cudaEventRecord(r->t0, st);
   for (int c = 0; c < NCLASS && !err; c++) {
     if (!cls_n[c]) continue;
     const int full = c >> 1, mode = c & 1;
@@ -1168,6 +1204,7 @@ static int issue_round(flam3gpu_service *s) {
     s->c_launches++;
     if (e) err = 1;
   }
+  cudaEventRecord(r->t1, st);
   cudaEventRecord(r->ev, st);
   cudaEventRecord(s->ev_last[si], st);
   r->in_use = 1;
@@ -1189,11 +1226,17 @@ static int issue_round(flam3gpu_service *s) {
   return 1;
 }
 
+static void round_done(flam3gpu_service *s, round_buf *r) {
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, r->t0, r->t1) == cudaSuccess) s->g_iter += ms * 1e-3;
+  r->in_use = 0;
+}
+
 static int rounds_in_flight(flam3gpu_service *s) {
   int n = 0;
   for (int k = 0; k < NRB; k++)
     if (s->rb[k].in_use) {
-      if (cudaEventQuery(s->rb[k].ev) == cudaSuccess) s->rb[k].in_use = 0;
+      if (cudaEventQuery(s->rb[k].ev) == cudaSuccess) round_done(s, &s->rb[k]);
       else n++;
     }
   return n;
@@ -1204,7 +1247,7 @@ static void wait_oldest_round(flam3gpu_service *s) {
     round_buf *r = &s->rb[k % NRB];
     if (r->in_use) {
       cudaEventSynchronize(r->ev);
-      r->in_use = 0;
+      round_done(s, r);
       return;
     }
   }
@@ -1222,7 +1265,7 @@ static void wait_oldest_tail(flam3gpu_service *s) {
 
 /* admits queued jobs while they fit; called with s->mu held */
 static void admit_pending(flam3gpu_service *s) {
-  while (s->pend_head && !s->paused) {
+  while (s->pend_head) {
     f3g_job *j = s->pend_head;
     if (s->cfg.max_active > 0 && s->nactive >= s->cfg.max_active) return;
     if (j->dev_bytes > s->budget) {
@@ -1248,7 +1291,9 @@ static void admit_pending(flam3gpu_service *s) {
     if (!s->pend_head) s->pend_tail = NULL;
     j->next = NULL;
     pthread_mutex_unlock(&s->mu);
+    const double ta = now_s();
     const int a = admit_job(s, j);
+    s->h_admit += now_s() - ta;
     pthread_mutex_lock(&s->mu);
     if (a == 2) {
       /* the pool has no room yet: back to the queue head until a job ends */
@@ -1285,20 +1330,36 @@ static void *service_main(void *arg) {
     pthread_mutex_lock(&s->mu);
     admit_pending(s);
     pthread_mutex_unlock(&s->mu);
+    double t0 = now_s();
     poll_tails(s);
-    if (rounds_in_flight(s) >= MAX_INFLIGHT) wait_oldest_round(s);
-    if (issue_round(s)) continue;
+    s->h_done += now_s() - t0;
+    if (rounds_in_flight(s) >= MAX_INFLIGHT) {
+      t0 = now_s();
+      wait_oldest_round(s);
+      s->h_wait += now_s() - t0;
+    }
+    t0 = now_s();
+    const int issued = issue_round(s);
+    s->h_round += now_s() - t0;
+    if (issued) continue;
     /* nothing to issue: wait for the GPU, or for submissions */
-    if (poll_tails(s) > 0) {
+    t0 = now_s();
+    const int busy = poll_tails(s);
+    s->h_done += now_s() - t0;
+    if (busy > 0) {
+      t0 = now_s();
       wait_oldest_tail(s);
+      s->h_wait += now_s() - t0;
       continue;
     }
     if (rounds_in_flight(s)) {
+      t0 = now_s();
       wait_oldest_round(s);
+      s->h_wait += now_s() - t0;
       continue;
     }
     pthread_mutex_lock(&s->mu);
-    if (s->nactive == 0 && (!s->pend_head || s->paused)) {
+    if (s->nactive == 0 && !s->pend_head) {
       if (s->stop) {
         pthread_mutex_unlock(&s->mu);
         break;
@@ -1353,6 +1414,7 @@ int flam3gpu_service_wait(flam3gpu_service *s, uint64_t ticket, double timeout_m
   s->jobs[ticket - 1] = NULL;
   pthread_mutex_unlock(&s->mu);
   int rv = j->rv;
+  if (rv == 0) copy_out(j);
   if (stats) *stats = j->stats;
   if (times_ms) {
     times_ms[0] = j->t_admit > 0 ? 1e3 * (j->t_admit - j->t_submit) : -1;
@@ -1382,8 +1444,8 @@ int flam3gpu_service_drain(flam3gpu_service *s) {
   return 0;
 }
 
-void flam3gpu_service_counters(flam3gpu_service *s, double out[12]) {
-  memset(out, 0, 12 * sizeof(double));
+void flam3gpu_service_counters(flam3gpu_service *s, double out[19]) {
+  memset(out, 0, 19 * sizeof(double));
   if (!s) return;
   pthread_mutex_lock(&s->mu);
   out[0] = s->c_done;
@@ -1398,6 +1460,13 @@ void flam3gpu_service_counters(flam3gpu_service *s, double out[12]) {
   out[9] = s->t_last_done > s->t_first_admit ? s->t_last_done - s->t_first_admit : 0;
   out[10] = s->c_h2d;
   out[11] = s->c_d2h;
+  out[12] = s->h_admit;
+  out[13] = s->h_round;
+  out[14] = s->h_tail;
+  out[15] = s->h_done;
+  out[16] = s->h_wait;
+  out[17] = s->g_iter;
+  out[18] = s->g_tail;
   pthread_mutex_unlock(&s->mu);
 }
 
@@ -1415,6 +1484,7 @@ void flam3gpu_service_destroy(flam3gpu_service *s) {
   }
   for (uint64_t t = 0; t < s->next_ticket; t++)
     if (s->jobs && s->jobs[t]) {
+      if (s->jobs[t]->h_out) pin_put(s->jobs[t]->h_out, align256(s->jobs[t]->out_bytes) + 2 * sizeof(unsigned long long));
       job_free_plan(s->jobs[t]);
       free(s->jobs[t]);
     }
@@ -1427,20 +1497,17 @@ void flam3gpu_service_destroy(flam3gpu_service *s) {
     if (s->rb[k].d_prefix) cudaFree(s->rb[k].d_prefix);
     if (s->rb[k].d_ctr) cudaFree(s->rb[k].d_ctr);
     if (s->rb[k].ev) cudaEventDestroy(s->rb[k].ev);
+    if (s->rb[k].t0) cudaEventDestroy(s->rb[k].t0);
+    if (s->rb[k].t1) cudaEventDestroy(s->rb[k].t1);
   }
   for (int k = 0; k < NTAIL; k++) {
     if (s->ts[k].ev) cudaEventDestroy(s->ts[k].ev);
+    if (s->ts[k].t0) cudaEventDestroy(s->ts[k].t0);
     free(s->ts[k].jobs);
   }
   for (int k = 0; k < NGRAPH; k++)
     if (s->graphs[k].exec) cudaGraphExecDestroy(s->graphs[k].exec);
-  for (int c = 0; c < 40; c++)
-    while (s->pin_free[c]) {
-      struct pin_buf *b = s->pin_free[c];
-      s->pin_free[c] = b->next;
-      cudaFreeHost(b->p);
-      free(b);
-    }
+
   for (int k = 0; k < 8; k++) {
     if (s->s_iter[k]) cudaStreamDestroy(s->s_iter[k]);
     if (s->ev_last[k]) cudaEventDestroy(s->ev_last[k]);
@@ -1475,12 +1542,16 @@ static void *submit_worker(void *p) {
   return NULL;
 }
 
-/* plans every frame (on up to 16 host threads), then releases them together */
-static int submit_all(flam3gpu_service *s, flam3_frame *frames, int n, void **outs, int field, int nchan, int transp,
-                      uint64_t *tk) {
-  pthread_mutex_lock(&s->mu);
-  s->paused = 1;
-  pthread_mutex_unlock(&s->mu);
+/* plans the frames on up to 16 host threads; each is admitted as soon as it
+ * is planned, so the device starts on the first while the rest are planned */
+int flam3gpu_service_submit_many(flam3gpu_service *s, flam3_frame *frames, int n, void **outs, int field, int nchan,
+                                 int transp, uint64_t *tk) {
+  f3g_clear_error();
+  if (!s || n < 0 || (n > 0 && (!frames || !outs || !tk))) {
+    f3g_set_error("bad arguments to flam3gpu_service_submit_many");
+    return 1;
+  }
+  if (n == 0) return 0;
   int nt = n < 16 ? n : 16;
   submit_arg *args = (submit_arg *)calloc((size_t)nt, sizeof(submit_arg));
   pthread_t *th = (pthread_t *)calloc((size_t)nt, sizeof(pthread_t));
@@ -1499,10 +1570,6 @@ static int submit_all(flam3gpu_service *s, flam3_frame *frames, int n, void **ou
   free(args);
   free(th);
   free(started);
-  pthread_mutex_lock(&s->mu);
-  s->paused = 0;
-  pthread_cond_broadcast(&s->cv_work);
-  pthread_mutex_unlock(&s->mu);
   return rv;
 }
 
@@ -1519,7 +1586,7 @@ int flam3gpu_render_batch(flam3_frame *frames, int n, void **outs, int field, in
   flam3gpu_service *s = flam3gpu_service_create(&c);
   if (!s) return 1;
   uint64_t *tk = (uint64_t *)calloc((size_t)n, sizeof(uint64_t));
-  int rv = submit_all(s, frames, n, outs, field, nchan, transp, tk);
+  int rv = flam3gpu_service_submit_many(s, frames, n, outs, field, nchan, transp, tk);
   char first_err[256] = "";
   for (int i = 0; i < n; i++) {
     if (!tk[i]) continue;

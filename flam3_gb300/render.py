@@ -13,7 +13,9 @@ import numpy as np
 from . import abi
 
 _LIB = None
-_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libflam3gpu.so")
+# FLAM3GPU_LIB selects another build of the library (see flam3_gb300._build --out)
+_LIB_PATH = os.environ.get("FLAM3GPU_LIB") or os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                                                            "libflam3gpu.so")
 
 
 class Flam3GpuError(RuntimeError):

@@ -35,6 +35,8 @@ def _lib():
         lib.flam3gpu_service_create.argtypes = [C.POINTER(ServiceConfig)]
         lib.flam3gpu_service_create.restype = P
         lib.flam3gpu_service_submit.argtypes = [P, F, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint64)]
+        lib.flam3gpu_service_submit_many.argtypes = [P, F, C.c_int, C.POINTER(C.c_void_p), C.c_int, C.c_int,
+                                                     C.c_int, C.POINTER(C.c_uint64)]
         lib.flam3gpu_service_wait.argtypes = [P, C.c_uint64, C.c_double, S, C.POINTER(C.c_double)]
         lib.flam3gpu_service_drain.argtypes = [P]
         lib.flam3gpu_service_counters.argtypes = [P, C.POINTER(C.c_double)]
@@ -62,7 +64,9 @@ def config(**kw):
 
 
 COUNTER_NAMES = ("jobs_done", "jobs_failed", "rounds", "launches", "tail_graphs", "graphs_instantiated",
-                 "samples_plotted", "device_bytes", "peak_device_bytes", "busy_s", "h2d_bytes", "d2h_bytes")
+                 "samples_plotted", "device_bytes", "peak_device_bytes", "busy_s", "h2d_bytes", "d2h_bytes",
+                 "host_admit_s", "host_round_s", "host_tail_s", "host_complete_s", "host_wait_s",
+                 "gpu_iterate_s", "gpu_tail_s")
 
 
 class Service:
@@ -88,6 +92,23 @@ class Service:
         self._keep[t.value] = out
         return t.value
 
+    def submit_many(self, frames, field=0, nchan=3, transp=0):
+        """Queues a list of frames planned in parallel and admitted together;
+        returns their tickets."""
+        n = len(frames)
+        arr = (abi.flam3_frame * n)(*[F.f for F in frames])
+        outs = [F.out_buffer(nchan) for F in frames]
+        ptrs = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
+        tk = (C.c_uint64 * n)()
+        r = self.lib.flam3gpu_service_submit_many(self.h, arr, n, ptrs, field, nchan, transp, tk)
+        for i, F in enumerate(frames):
+            F.f.rc = arr[i].rc
+            if tk[i]:
+                self._keep[tk[i]] = outs[i]
+        if r:
+            raise render.Flam3GpuError("submit_many failed: " + self.lib.flam3gpu_last_error().decode())
+        return list(tk)
+
     def wait(self, ticket, timeout_ms=-1.0):
         """(image, stats, times_ms) of a finished job; times_ms = [submit->admit,
         admit->first round, latency, rounds]."""
@@ -105,7 +126,7 @@ class Service:
         self.lib.flam3gpu_service_drain(self.h)
 
     def counters(self):
-        a = (C.c_double * 12)()
+        a = (C.c_double * 19)()
         self.lib.flam3gpu_service_counters(self.h, a)
         return dict(zip(COUNTER_NAMES, list(a)))
 

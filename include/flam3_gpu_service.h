@@ -66,6 +66,12 @@ flam3gpu_service *flam3gpu_service_create(const flam3gpu_service_config *cfg);
 int flam3gpu_service_submit(flam3gpu_service *s, flam3_frame *f, void *out, int field, int nchan, int transp,
                             uint64_t *ticket);
 
+/* Queues n renders at once: they are planned on up to 16 host threads and
+ * admitted together, so one round can hold all of them.  tickets[i] is 0
+ * for a frame whose planning failed (the call then returns 1). */
+int flam3gpu_service_submit_many(flam3gpu_service *s, flam3_frame *frames, int n, void **outs, int field, int nchan,
+                                 int transp, uint64_t *tickets);
+
 /* Waits for a job (timeout_ms < 0: no limit).  Returns 0 when it finished
  * successfully (stats filled like flam3_render's), 1 when it failed, 2 on
  * timeout.  times_ms (may be NULL) receives [0] submit -> admitted,
@@ -81,8 +87,13 @@ int flam3gpu_service_drain(flam3gpu_service *s);
  * [3] kernel launches, [4] tail graphs launched, [5] tail graphs
  * instantiated, [6] samples plotted, [7] device bytes in use, [8] peak device
  * bytes, [9] busy seconds (first admission to last completion),
- * [10] host-to-device bytes, [11] device-to-host bytes. */
-void flam3gpu_service_counters(flam3gpu_service *s, double out[12]);
+ * [10] host-to-device bytes, [11] device-to-host bytes; service-thread
+ * seconds spent [12] admitting jobs, [13] building and launching rounds,
+ * [14] capturing and launching tails, [15] completing jobs (copy-out),
+ * [16] waiting for the GPU; device seconds (CUDA events) of [17] iterate
+ * rounds and [18] tails (rounds on different streams overlap, so [17] can
+ * exceed the wall time). */
+void flam3gpu_service_counters(flam3gpu_service *s, double out[19]);
 
 /* Waits for all jobs and releases the service. */
 void flam3gpu_service_destroy(flam3gpu_service *s);
