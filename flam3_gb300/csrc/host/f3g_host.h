@@ -26,6 +26,23 @@ typedef struct {
 } f3g_geom;
 
 int f3g_geometry(flam3_frame *spec, const flam3_genome *cp, int field, double **filter, f3g_geom *g);
+
+/* per temporal sample results of f3g_build_batch_passes */
+typedef struct f3g_pass_info_s {
+  double vibrancy, gamma, background[3];
+  double sample_density, ppux, ppuy, batch_size;
+  double contrast, brightness, gam_lin_thresh, estimator_curve;
+  int need_count; /* palette alpha != 1 */
+  int err;
+  char errmsg[256];
+} f3g_pass_info;
+
+/* The passes of batch `batch` (its ntemporal temporal samples): keys drawn
+ * in order from spec->rc, then each sample's genome interpolated, prepared
+ * and packed (host threads); per-sample scalars in info[]. */
+int f3g_build_batch_passes(flam3_frame *spec, int field, const f3g_geom *g, int batch, int nbatches, int ntemporal,
+                           const double *tfilter, const double *tdeltas, int cmap_size, F3GPass *passes,
+                           f3g_pass_info *info);
 int f3g_camera(flam3_frame *spec, const flam3_genome *cp, int field, const f3g_geom *g, F3GPass *p,
                double *sample_density, double *ppux, double *ppuy);
 void f3g_pass_key(flam3_frame *spec, uint32_t key[2]);
@@ -75,6 +92,7 @@ typedef struct {
   F3GPass *h_passes; size_t h_passes_bytes; /* pinned */
   long long *d_prefix; size_t prefix_bytes; long long *h_prefix; size_t prefix_n;
   F3GItem *d_items; size_t d_items_bytes; F3GItem *h_items; size_t h_items_n; /* pinned */
+  struct f3g_pass_info_s *h_info; size_t h_info_n;
   F3GCounters *d_ctr; F3GCounters *h_ctr;
   float *d_filter; size_t filter_bytes;
   float *d_de_w; size_t de_w_bytes;

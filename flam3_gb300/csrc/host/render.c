@@ -15,6 +15,7 @@
  */
 #define _GNU_SOURCE
 #include <math.h>
+#include <pthread.h>
 #include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -91,6 +92,15 @@ static int ensure_host_passes(f3g_ctx *c, size_t n) {
       return 1;
     }
     c->prefix_n = n + 1;
+  }
+  if (!(c->h_info && c->h_info_n >= n)) {
+    free(c->h_info);
+    c->h_info = (f3g_pass_info *)calloc(n, sizeof(f3g_pass_info));
+    c->h_info_n = c->h_info ? n : 0;
+    if (!c->h_info) {
+      f3g_set_error("host memory exhausted");
+      return 1;
+    }
   }
   if (!(c->h_items && c->h_items_n >= n)) {
     if (c->h_items) cudaFreeHost(c->h_items);
@@ -235,6 +245,108 @@ static unsigned long irand(randctx *r) {
     r->randcnt = F3_RANDSIZ - 1;
   }
   return r->randrsl[r->randcnt];
+}
+
+/* ---- building the passes of one batch (rect.c:754-827) ----
+ * The Philox keys are drawn first, in temporal-sample order, from the
+ * caller's ISAAC context (the only ordered step); the genome interpolation,
+ * preparation and packing of each temporal sample are independent and run on
+ * up to 16 host threads; the per-sample scalars are summed afterwards in
+ * order, so the result does not depend on the thread count. */
+typedef struct {
+  flam3_frame *spec;
+  const f3g_geom *g;
+  int field, first, ntemporal, nbatches, cmap_size, stride, start;
+  const double *tfilter, *tdeltas;
+  F3GPass *passes;
+  f3g_pass_info *info;
+} pass_job;
+
+static void build_one_pass(const pass_job *pj, int ts) {
+  F3GPass *p = &pj->passes[ts];
+  f3g_pass_info *in = &pj->info[ts];
+  flam3_frame *spec = pj->spec;
+  flam3_genome cp;
+  memset(&cp, 0, sizeof(cp));
+  const int gi = pj->first + ts;
+  const double color_scalar = pj->tfilter[gi];
+  const double tst = spec->time + pj->tdeltas[gi];
+  uint32_t key0 = p->key[0], key1 = p->key[1];
+  memset(p, 0, offsetof(F3GPass, xf));
+  p->key[0] = key0;
+  p->key[1] = key1;
+  in->err = 1;
+  f3g_clear_error();
+  if (f3g_interpolate(spec->genomes, spec->ngenomes, tst, &cp) || f3g_prepare_precalc_flags(&cp) ||
+      f3g_build_distrib(&cp, p))
+    goto fail;
+  for (int i = 0; i < cp.num_xforms; i++) f3g_xform_precalc(&cp, i);
+  if (f3g_pack_genome(&cp, p)) goto fail;
+  in->need_count = 0;
+  for (int j = 0; j < 256; j++) {
+    for (int k = 0; k < 4; k++) p->dmap[j][k] = (float)((cp.palette[j].color[k] * F3G_WHITE) * color_scalar);
+    if (cp.palette[j].color[3] != 1.0) in->need_count = 1;
+  }
+  p->cmap_size = pj->cmap_size;
+  p->palette_mode = cp.palette_mode;
+  if (set_camera(spec, &cp, pj->field, pj->g, p, &in->sample_density, &in->ppux, &in->ppuy)) goto fail;
+  const double nsamples = in->sample_density * pj->g->image_width * pj->g->image_height;
+  in->batch_size = nsamples / (pj->nbatches * pj->ntemporal);
+  p->samples = (long long)in->batch_size;
+  p->fuse = spec->earlyclip ? 100 : 15;
+  p->iter_mode = (cp.chaos_enable || f3g_opts.iter_mode == 0) ? 0 : 1;
+  in->vibrancy = cp.vibrancy;
+  in->gamma = cp.gamma;
+  for (int k = 0; k < 3; k++) in->background[k] = cp.background[k];
+  in->contrast = cp.contrast;
+  in->brightness = cp.brightness;
+  in->gam_lin_thresh = cp.gam_lin_thresh;
+  in->estimator_curve = cp.estimator_curve;
+  in->err = 0;
+  f3g_genome_free(&cp);
+  return;
+fail:
+  snprintf(in->errmsg, sizeof(in->errmsg), "%s", flam3gpu_last_error());
+  f3g_genome_free(&cp);
+}
+
+static void *pass_worker(void *arg) {
+  const pass_job *pj = (const pass_job *)arg;
+  for (int ts = pj->start; ts < pj->ntemporal; ts += pj->stride) build_one_pass(pj, ts);
+  return NULL;
+}
+
+int f3g_build_batch_passes(flam3_frame *spec, int field, const f3g_geom *g, int batch, int nbatches, int ntemporal,
+                           const double *tfilter, const double *tdeltas, int cmap_size, F3GPass *passes,
+                           f3g_pass_info *info) {
+  /* keys in order: the caller's ISAAC context advances as the reference's */
+  for (int ts = 0; ts < ntemporal; ts++) consume_rc(spec, passes[ts].key);
+  int nt = ntemporal / 4;
+  if (nt > 16) nt = 16;
+  if (nt < 1) nt = 1;
+  pass_job pj = {spec, g, field, batch * ntemporal, ntemporal, nbatches, cmap_size, 1, 0, tfilter, tdeltas, passes, info};
+  if (nt == 1) {
+    pass_worker(&pj);
+  } else {
+    pthread_t th[16];
+    pass_job jobs[16];
+    int started[16];
+    for (int k = 0; k < nt; k++) {
+      jobs[k] = pj;
+      jobs[k].stride = nt;
+      jobs[k].start = k;
+      started[k] = pthread_create(&th[k], NULL, pass_worker, &jobs[k]) == 0;
+      if (!started[k]) pass_worker(&jobs[k]);
+    }
+    for (int k = 0; k < nt; k++)
+      if (started[k]) pthread_join(th[k], NULL);
+  }
+  for (int ts = 0; ts < ntemporal; ts++)
+    if (info[ts].err) {
+      f3g_set_error("%s", info[ts].errmsg[0] ? info[ts].errmsg : "pass preparation failed");
+      return 1;
+    }
+  return 0;
 }
 
 static float *upload_floats(f3g_ctx *c, float **dptr, size_t *cap, const double *src, size_t n) {
@@ -392,41 +504,33 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
     }
     /* ---- passes of this batch ---- */
     long long total_chunks = 0, batch_samples = 0;
+    if (f3g_build_batch_passes(spec, field, &g, batch, nbatches, ntemporal, tfilter, tdeltas, cmap_size, c->h_passes,
+                               c->h_info))
+      goto done;
     for (int ts = 0; ts < ntemporal; ts++) {
-      double color_scalar = tfilter[batch * ntemporal + ts];
-      double tst = spec->time + tdeltas[batch * ntemporal + ts];
       F3GPass *p = &c->h_passes[ts];
-      memset(p, 0, offsetof(F3GPass, xf));
-      if (f3g_interpolate(spec->genomes, spec->ngenomes, tst, &cp)) goto done;
-      if (f3g_prepare_precalc_flags(&cp)) goto done;
-      if (f3g_build_distrib(&cp, p)) goto done;
-      for (int i = 0; i < cp.num_xforms; i++) f3g_xform_precalc(&cp, i);
-      if (f3g_pack_genome(&cp, p)) goto done;
-      for (int j = 0; j < 256; j++) {
-        for (int k = 0; k < 4; k++) p->dmap[j][k] = (float)((cp.palette[j].color[k] * F3G_WHITE) * color_scalar);
-        if (cp.palette[j].color[3] != 1.0) need_count = 1;
-      }
-      p->cmap_size = cmap_size;
-      p->palette_mode = cp.palette_mode;
-      if (set_camera(spec, &cp, field, &g, p, &sample_density, &ppux, &ppuy)) goto done;
-      double nsamples = sample_density * g.image_width * g.image_height;
-      double batch_size = nsamples / (nbatches * ntemporal);
-      stats->num_iters += batch_size;
-      p->samples = (long long)batch_size;
-      p->fuse = spec->earlyclip ? 100 : 15;
-      p->iter_mode = (cp.chaos_enable || f3g_opts.iter_mode == 0) ? 0 : 1;
+      const f3g_pass_info *in = &c->h_info[ts];
+      need_count |= in->need_count;
+      sample_density = in->sample_density;
+      ppux = in->ppux;
+      ppuy = in->ppuy;
+      stats->num_iters += in->batch_size;
       p->buckets = c->d_hist;
       p->count = use_count ? c->d_count : NULL;
       p->bucket_kind = bkind;
-      consume_rc(spec, p->key);
       batch_samples += p->samples;
-      vibrancy += cp.vibrancy;
-      gamma += cp.gamma;
-      background[0] += cp.background[0];
-      background[1] += cp.background[1];
-      background[2] += cp.background[2];
+      vibrancy += in->vibrancy;
+      gamma += in->gamma;
+      background[0] += in->background[0];
+      background[1] += in->background[1];
+      background[2] += in->background[2];
       vib_gam_n++;
     }
+    /* k1/k2, the DE curve and the tonemap read the last temporal sample's genome */
+    cp.contrast = c->h_info[ntemporal - 1].contrast;
+    cp.brightness = c->h_info[ntemporal - 1].brightness;
+    cp.gam_lin_thresh = c->h_info[ntemporal - 1].gam_lin_thresh;
+    cp.estimator_curve = c->h_info[ntemporal - 1].estimator_curve;
     if (use_count == 0 && de_on && need_count) {
       /* palette alpha != 1 found while packing: redo the batch with a count plane */
       use_count = 1;

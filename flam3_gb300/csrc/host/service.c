@@ -44,7 +44,6 @@
 #define NBRANCH 4     /* parallel branches of a tail graph */
 #define NCLASS 4      /* kernel classes: full variations x xform-choice mode */
 #define NGRAPH 8      /* cached executable tail graphs */
-#define MAX_INFLIGHT 2
 
 enum { J_QUEUED = 0, J_ACTIVE, J_DONE, J_FAILED };
 enum { P_ITER = 0, P_TAIL, P_WAIT_UP };
@@ -306,6 +305,7 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
   if (f3g_interpolate(spec->genomes, spec->ngenomes, spec->time, &cp)) return 1;
   int rv = 1;
   double *filter = NULL, *tfilter = NULL, *tdeltas = NULL, *de_w = NULL, *de_c = NULL;
+  f3g_pass_info *info = NULL;
   const int nbatches = cp.nbatches, ntemporal = cp.ntemporal_samples;
   const double highpow = cp.highlight_power;
   j->nbatches = nbatches;
@@ -340,7 +340,8 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
   j->pass_prefix = (long long *)calloc((size_t)nbatches * (ntemporal + 1), sizeof(long long));
   j->bp = (batch_plan *)calloc((size_t)nbatches, sizeof(batch_plan));
   j->h_filter = (float *)malloc((size_t)g.filter_width * g.filter_width * sizeof(float));
-  if (!j->h_passes || !j->pass_prefix || !j->bp || !j->h_filter) {
+  info = (f3g_pass_info *)calloc((size_t)ntemporal, sizeof(f3g_pass_info));
+  if (!j->h_passes || !j->pass_prefix || !j->bp || !j->h_filter || !info) {
     f3g_set_error("host memory exhausted");
     goto done;
   }
@@ -391,40 +392,32 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
     }
     long long batch_samples = 0;
     int full = 0, mode = 1;
+    F3GPass *bpass = &j->h_passes[batch * ntemporal];
+    if (f3g_build_batch_passes(spec, field, &g, batch, nbatches, ntemporal, tfilter, tdeltas, cmap_size, bpass, info))
+      goto done;
     for (int ts = 0; ts < ntemporal; ts++) {
-      const double color_scalar = tfilter[batch * ntemporal + ts];
-      const double tst = spec->time + tdeltas[batch * ntemporal + ts];
-      F3GPass *p = &j->h_passes[batch * ntemporal + ts];
-      if (f3g_interpolate(spec->genomes, spec->ngenomes, tst, &cp)) goto done;
-      if (f3g_prepare_precalc_flags(&cp)) goto done;
-      if (f3g_build_distrib(&cp, p)) goto done;
-      for (int i = 0; i < cp.num_xforms; i++) f3g_xform_precalc(&cp, i);
-      if (f3g_pack_genome(&cp, p)) goto done;
-      for (int q = 0; q < 256; q++) {
-        for (int k = 0; k < 4; k++) p->dmap[q][k] = (float)((cp.palette[q].color[k] * F3G_WHITE) * color_scalar);
-        if (cp.palette[q].color[3] != 1.0) need_count = 1;
-      }
-      p->cmap_size = cmap_size;
-      p->palette_mode = cp.palette_mode;
-      if (f3g_camera(spec, &cp, field, &g, p, &sample_density, &ppux, &ppuy)) goto done;
-      const double nsamples = sample_density * g.image_width * g.image_height;
-      const double batch_size = nsamples / (nbatches * ntemporal);
-      j->stats.num_iters += batch_size;
-      p->samples = (long long)batch_size;
-      p->fuse = spec->earlyclip ? 100 : 15;
-      p->iter_mode = (cp.chaos_enable || f3g_opts.iter_mode == 0) ? 0 : 1;
+      F3GPass *p = &bpass[ts];
+      const f3g_pass_info *in = &info[ts];
+      need_count |= in->need_count;
+      sample_density = in->sample_density;
+      ppux = in->ppux;
+      ppuy = in->ppuy;
+      j->stats.num_iters += in->batch_size;
       p->bucket_kind = j->bkind;
-      f3g_pass_key(spec, p->key);
       batch_samples += p->samples;
       full |= p->full_variations;
       if (p->iter_mode == 0) mode = 0;
-      vibrancy += cp.vibrancy;
-      gamma += cp.gamma;
-      background[0] += cp.background[0];
-      background[1] += cp.background[1];
-      background[2] += cp.background[2];
+      vibrancy += in->vibrancy;
+      gamma += in->gamma;
+      background[0] += in->background[0];
+      background[1] += in->background[1];
+      background[2] += in->background[2];
       vib_gam_n++;
     }
+    cp.contrast = info[ntemporal - 1].contrast;
+    cp.brightness = info[ntemporal - 1].brightness;
+    cp.gam_lin_thresh = info[ntemporal - 1].gam_lin_thresh;
+    cp.estimator_curve = info[ntemporal - 1].estimator_curve;
     b->use_count = b->de_on && need_count;
     j->count_any |= b->use_count;
     b->full = full;
@@ -523,6 +516,7 @@ done:
   free(tdeltas);
   free(de_w);
   free(de_c);
+  free(info);
   f3g_genome_free(&cp);
   return rv;
 }
@@ -534,6 +528,7 @@ void flam3gpu_service_default_config(flam3gpu_service_config *cfg) {
   cfg->tail_graphs = 1;
   cfg->streams = 2;
   cfg->use_tuning = 1;
+  cfg->max_inflight = 2;
 }
 
 static void *service_main(void *arg);
@@ -557,6 +552,8 @@ flam3gpu_service *flam3gpu_service_create(const flam3gpu_service_config *cfg_in)
   else flam3gpu_service_default_config(&s->cfg);
   if (s->cfg.streams < 1) s->cfg.streams = 2;
   if (s->cfg.streams > 8) s->cfg.streams = 8;
+  if (s->cfg.max_inflight < 1) s->cfg.max_inflight = 2;
+  if (s->cfg.max_inflight > NRB - 1) s->cfg.max_inflight = NRB - 1;
   if (cudaGetDevice(&s->device) != cudaSuccess ||
       cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device) != cudaSuccess) {
     f3g_set_error("no CUDA device available");
@@ -1087,8 +1084,21 @@ static int issue_round(flam3gpu_service *s) {
     return ntails > 0;
   }
   qsort(cand, (size_t)nc, sizeof(f3g_job *), job_remaining_cmp);
-  /* shortest remaining job first, up to the round's sample budget */
-  double budget = s->cfg.round_samples < 0 ? 1e300 : s->cfg.round_samples > 0 ? (double)s->cfg.round_samples : 2.0e8;
+  /* shortest remaining job first, up to the round's sample budget; the
+   * automatic budget gives every resident block at least 4 chunks of the
+   * coarsest job, so the round's last wave wastes little */
+  double budget;
+  if (s->cfg.round_samples < 0) budget = 1e300;
+  else if (s->cfg.round_samples > 0) budget = (double)s->cfg.round_samples;
+  else {
+    double cmax = 0;
+    for (int i = 0; i < nc; i++) {
+      const double cs = (double)cand[i]->threads * cand[i]->bp[cand[i]->batch].S;
+      if (cs > cmax) cmax = cs;
+    }
+    budget = 4.0 * cmax * s->nsm * 4;
+    if (budget < 2.0e8) budget = 2.0e8;
+  }
   int np = 0;
   for (int i = 0; i < nc && budget > 0; i++, np++) {
     f3g_job *j = cand[i];
@@ -1333,7 +1343,7 @@ static void *service_main(void *arg) {
     double t0 = now_s();
     poll_tails(s);
     s->h_done += now_s() - t0;
-    if (rounds_in_flight(s) >= MAX_INFLIGHT) {
+    if (rounds_in_flight(s) >= s->cfg.max_inflight) {
       t0 = now_s();
       wait_oldest_round(s);
       s->h_wait += now_s() - t0;

@@ -45,13 +45,14 @@ typedef struct flam3gpu_service flam3gpu_service;
 
 typedef struct {
   double hbm_budget_bytes;  /* device bytes held for job buffers (0: 150 GB or 90% of free memory) */
-  long long round_samples;  /* samples per iterate round (0: automatic, about 10 ms of work;
-                               -1: one round holds all admitted work) */
+  long long round_samples;  /* samples per iterate round (0: automatic -- at least 2e8 samples and
+                               4 chunks per resident block; -1: one round holds all admitted work) */
   int max_active;           /* admitted jobs at once (0: unlimited) */
   int tail_graphs;          /* 1: per-round tail in a CUDA graph (default); 0: direct launches */
   int streams;              /* iterate streams rounds alternate over (default 2) */
   int use_tuning;           /* 1: apply the autotuned table (flam3gpu_autotune) to new jobs */
-  int reserved[8];
+  int max_inflight;         /* iterate rounds queued on the device at once (default 2) */
+  int reserved[7];
 } flam3gpu_service_config;
 
 void flam3gpu_service_default_config(flam3gpu_service_config *cfg);
