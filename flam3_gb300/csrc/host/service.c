@@ -526,9 +526,10 @@ done:
 void flam3gpu_service_default_config(flam3gpu_service_config *cfg) {
   memset(cfg, 0, sizeof(*cfg));
   cfg->tail_graphs = 1;
-  cfg->streams = 2;
+  cfg->streams = 1;
   cfg->use_tuning = 1;
   cfg->max_inflight = 2;
+  cfg->tail_branches = 1;
 }
 
 static void *service_main(void *arg);
@@ -550,10 +551,12 @@ flam3gpu_service *flam3gpu_service_create(const flam3gpu_service_config *cfg_in)
   }
   if (cfg_in) s->cfg = *cfg_in;
   else flam3gpu_service_default_config(&s->cfg);
-  if (s->cfg.streams < 1) s->cfg.streams = 2;
+  if (s->cfg.streams < 1) s->cfg.streams = 1;
   if (s->cfg.streams > 8) s->cfg.streams = 8;
   if (s->cfg.max_inflight < 1) s->cfg.max_inflight = 2;
   if (s->cfg.max_inflight > NRB - 1) s->cfg.max_inflight = NRB - 1;
+  if (s->cfg.tail_branches < 1) s->cfg.tail_branches = 1;
+  if (s->cfg.tail_branches > NBRANCH) s->cfg.tail_branches = NBRANCH;
   if (cudaGetDevice(&s->device) != cudaSuccess ||
       cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device) != cudaSuccess) {
     f3g_set_error("no CUDA device available");
@@ -909,14 +912,14 @@ static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n) {
       cudaEventRecord(s->ev_fork, s->s_tail);
       int used[NBRANCH] = {0};
       for (int i = 0; i < n && !err; i++) {
-        const int k = i % NBRANCH;
+        const int k = i % s->cfg.tail_branches;
         if (!used[k]) {
           cudaStreamWaitEvent(s->s_br[k], s->ev_fork, 0);
           used[k] = 1;
         }
-        char bs[8];
+        char bs[16];
         snprintf(bs, sizeof(bs), "%d:", k);
-        if (strlen(sig) + 4 < sizeof(sig)) strcat(sig, bs);
+        if (strlen(sig) + strlen(bs) + 1 < sizeof(sig)) strcat(sig, bs);
         err = enqueue_tail_ops(s, jobs[i], s->s_br[k], sig, sizeof(sig));
       }
       for (int k = 0; k < NBRANCH; k++)

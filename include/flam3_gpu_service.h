@@ -11,13 +11,11 @@
  *     the service's HBM budget;
  *   - the scheduler runs iteration in rounds: each round is one persistent
  *     iterate-and-accumulate launch over slices of every admitted job's
- *     temporal samples (per-job work lists in one chunk queue), with
- *     consecutive rounds on alternating streams so a round's last blocks
- *     overlap the next round's first;
+ *     temporal samples (per-job work lists in one chunk queue), shortest
+ *     remaining job first; rounds may alternate over several streams;
  *   - jobs whose iteration finished in a round get their density
- *     estimation / filter / tonemap / copy-out in one CUDA graph per round
- *     (parallel branches, one per job), replayed with updated parameters
- *     when the round's shape repeats;
+ *     estimation / filter / tonemap / copy-out in one CUDA graph per round,
+ *     updated in place when a later round's tail has the same shape;
  *   - requests that arrive while others run join at the next round
  *     (continuous batching); histograms, pass tables and chunk cursors stay
  *     resident on the device between rounds.
@@ -49,10 +47,12 @@ typedef struct {
                                4 chunks per resident block; -1: one round holds all admitted work) */
   int max_active;           /* admitted jobs at once (0: unlimited) */
   int tail_graphs;          /* 1: per-round tail in a CUDA graph (default); 0: direct launches */
-  int streams;              /* iterate streams rounds alternate over (default 2) */
+  int streams;              /* iterate streams rounds alternate over (default 1; with 2 the next
+                               round's blocks fill the SMs a draining round frees) */
   int use_tuning;           /* 1: apply the autotuned table (flam3gpu_autotune) to new jobs */
   int max_inflight;         /* iterate rounds queued on the device at once (default 2) */
-  int reserved[7];
+  int tail_branches;        /* parallel branches of a round's tail graph (default 1: one chain) */
+  int reserved[6];
 } flam3gpu_service_config;
 
 void flam3gpu_service_default_config(flam3gpu_service_config *cfg);

@@ -59,7 +59,7 @@ def test_service_config_defaults_without_gpu():
     from flam3_gb300 import service
 
     c = service.config()
-    assert c.tail_graphs == 1 and c.streams == 2 and c.use_tuning == 1
+    assert c.tail_graphs == 1 and c.streams == 1 and c.use_tuning == 1 and c.tail_branches == 1
     assert c.round_samples == 0 and c.hbm_budget_bytes == 0.0
     c = service.config(round_samples=-1, streams=3)
     assert c.round_samples == -1 and c.streams == 3
