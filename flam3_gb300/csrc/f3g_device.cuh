@@ -133,9 +133,37 @@ __device__ __forceinline__ double m_log(double x) { return log(x); }
 __device__ __forceinline__ double m_pow(double x, double y) { return pow(x, y); }
 __device__ __forceinline__ float m_tan(float x) { return tanf(x); }
 __device__ __forceinline__ double m_tan(double x) { return tan(x); }
+#ifdef F3G_FAST_MATH
+/* atan2 from atan on [0, 1] by octant reduction; atan(a) ~ a * P(a^2), P of
+ * degree 6 fitted to arctangent on [0, 1] by iteratively reweighted least
+ * squares (Lawson) for this project: max abs error 2.5e-7 rad. */
+__device__ __forceinline__ float m_atan2(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+  const float a = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
+  const float s = a * a;
+  float p = 0.006811756f;
+  p = fmaf(p, s, -0.033604111f);
+  p = fmaf(p, s, 0.079623550f);
+  p = fmaf(p, s, -0.132333356f);
+  p = fmaf(p, s, 0.198078140f);
+  p = fmaf(p, s, -0.333173679f);
+  p = fmaf(p, s, 0.999996112f);
+  float r = a * p;
+  if (ay > ax) r = 1.57079632679489662f - r;
+  if (x < 0.0f) r = 3.14159265358979324f - r;
+  if (x != x || y != y) r = x + y;
+  return copysignf(r, y);
+}
+/* square root from the hardware reciprocal square root (about 3 ulp) */
+__device__ __forceinline__ float m_sqrt(float x) {
+  return x > 0.0f ? x * rsqrtf(x) : (x == 0.0f ? 0.0f : __int_as_float(0x7fc00000));
+}
+#else
 __device__ __forceinline__ float m_atan2(float y, float x) { return atan2f(y, x); }
-__device__ __forceinline__ double m_atan2(double y, double x) { return atan2(y, x); }
 __device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
+#endif
+__device__ __forceinline__ double m_atan2(double y, double x) { return atan2(y, x); }
 __device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float m_log10(float x) { return log10f(x); }
 __device__ __forceinline__ double m_log10(double x) { return log10(x); }

@@ -279,6 +279,8 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
   long long n_chunk = s.samples - base;
   if (n_chunk > (long long)T * S) n_chunk = (long long)T * S;
   long long q = n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0);
+  R *bx = reinterpret_cast<R *>(buf), *by = bx + T, *bc = by + T;
+  int *bq = reinterpret_cast<int *>(bc + T);
   Rng rng;
   rng.init(s.key0, s.key1, (uint32_t)local_chunk, (uint32_t)t, 0x5EEDu);
   WarpWords ww;
@@ -305,12 +307,17 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
       }
     }
     rot += 0x9E3779B1u * (uint32_t)(round + 1);
-    /* transpose lanes across warps, then rotate by a block-uniform amount */
-    int dst = ((lane * nwarps + (t >> 5)) + (int)(rot >> 20)) & (T - 1);
+    /* transpose lanes across warps, XOR the low five bits and rotate by
+     * whole 32-point segments (block-uniform amounts); points are stored
+     * structure-of-arrays at swizzled slots i ^ ((i >> 5) & 31), so both the
+     * transposed writes and the reads hit 32 distinct banks */
+    const int x5 = (int)(rot >> 27), k8 = (int)(rot >> 24) & 7;
+    const int dst = ((((lane * nwarps + (t >> 5)) ^ x5) + 32 * k8) & (T - 1));
+    const int wslot = dst ^ ((dst >> 5) & 31), rslot = t ^ ((t >> 5) & 31);
     __syncthreads();
-    buf[dst].x = px; buf[dst].y = py; buf[dst].c = pc; buf[dst].consec = consec;
+    bx[wslot] = px; by[wslot] = py; bc[wslot] = pc; bq[wslot] = consec;
     int more = __syncthreads_or(remaining > 0 || fuse_left > 0);
-    px = buf[t].x; py = buf[t].y; pc = buf[t].c; consec = buf[t].consec;
+    px = bx[rslot]; py = by[rslot]; pc = bc[rslot]; consec = bq[rslot];
     if (!more) break;
   }
   (void)po;
