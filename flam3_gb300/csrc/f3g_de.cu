@@ -50,8 +50,11 @@ struct DEParams {
   F3GTonemap tp;
 };
 
-/* sources with more taps than this inside the region go to the shared list */
+/* sources with more taps than this inside the region go to the shared list
+ * (one warp per source); fewer are scattered by the classifying thread */
+#ifndef DE_SMALL_TAPS
 #define DE_SMALL_TAPS 16
+#endif
 
 __device__ __forceinline__ float de_coef(float4 ki, int r2) {
   return (float)r2 <= ki.z ? ki.x * exp2f(ki.y * (float)r2) : 0.0f;

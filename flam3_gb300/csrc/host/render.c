@@ -465,6 +465,7 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
   if (f3g_ensure((void **)&c->d_prefix, &c->prefix_bytes, (size_t)(ntemporal + 1) * sizeof(long long))) goto done;
   if (f3g_ensure((void **)&c->d_items, &c->d_items_bytes, (size_t)ntemporal * sizeof(F3GItem))) goto done;
   const int precision = f3g_opts.iter_precision == 64 ? 64 : 32;
+  const int de_tile = f3g_opts.de_tile > 0 ? f3g_opts.de_tile : 16;
   double vibrancy = 0.0, gamma = 0.0, background[3] = {0, 0, 0};
   int vib_gam_n = 0;
   double ppux = 0, ppuy = 0, sample_density = 0;
@@ -684,7 +685,7 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         if (!ok) goto done;
       }
       h2d += (double)nk * 4 * sizeof(float);
-      if (fused_tail && f3g_de_fused_smem(g.oversample, g.filter_width, R, nk) <= 220 * 1024) {
+      if (fused_tail && f3g_de_fused_smem_tile(g.oversample, g.filter_width, R, nk, de_tile) <= 220 * 1024) {
         /* DE, filter, tonemap and pack in one kernel below */
         fde = 1;
         fde_mfc = mfc;
@@ -758,10 +759,10 @@ tail_fused:;
     CK(cudaEventRecord(c->ev[4], c->stream));
     int e;
     if (fde) {
-      e = f3g_launch_de_fused(c->d_hist, bkind, fde_count ? c->d_count : NULL, g.W, g.H, g.oversample, fde_k1,
+      e = f3g_launch_de_fused_tile(c->d_hist, bkind, fde_count ? c->d_count : NULL, g.W, g.H, g.oversample, fde_k1,
                               fde_k2, fde_curve, fde_mfc, fde_mfi, c->d_de_w, fde_R, g.de_offset,
                               c->d_filter, g.filter_width, g.image_width, g.image_height, c->d_out, spec->earlyclip,
-                              &tp, c->stream);
+                              &tp, de_tile, c->stream);
       launches++;
     } else if (fused_tail && !de_used_any) {
       double k1 = (cp.contrast * cp.brightness * 255.0 * 268.0 * 1.0) / 256;

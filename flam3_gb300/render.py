@@ -31,7 +31,7 @@ class RenderIO(C.Structure):
 class Options(C.Structure):
     _fields_ = [("iter_mode", C.c_int), ("iter_precision", C.c_int), ("shuffle_every", C.c_int),
                 ("threads_per_block", C.c_int), ("blocks", C.c_int), ("chain_samples", C.c_int),
-                ("seed_salt", C.c_uint64), ("reserved", C.c_int * 8)]
+                ("seed_salt", C.c_uint64), ("de_tile", C.c_int), ("reserved", C.c_int * 7)]
 
 
 def load():

@@ -230,7 +230,9 @@ const char *flam3gpu_version(void);
  * with non-unity xaos always use mode 0.  iter_precision: 32 or 64 (FP64
  * iteration, slow on GB300; parity work).  threads_per_block, blocks: 0 =
  * automatic.  chain_samples: samples per chain before a restart with a new
- * random point and fuse (0 = f->sub_batch_size, like the reference). */
+ * random point and fuse (0 = f->sub_batch_size, like the reference).
+ * de_tile: output pixels per tile edge of the fused density-estimation
+ * kernel (8 .. 32; 0 = 16). */
 typedef struct {
   int iter_mode;
   int iter_precision;
@@ -239,7 +241,8 @@ typedef struct {
   int blocks;
   int chain_samples;
   uint64_t seed_salt;
-  int reserved[8];
+  int de_tile;        /* output-tile edge of the fused DE kernel (0 = 16) */
+  int reserved[7];
 } flam3gpu_options;
 
 void flam3gpu_default_options(flam3gpu_options *o);
