@@ -54,6 +54,11 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 METRIC = "Giter/s; renders/s and p50/p99 latency, served vs plain, at matched image error"
 WORKLOAD = "config1 still: 1920x1080 q2000 ss2 DE r9 gaussian r1, 6 xforms + final, bits 33"
 CPU_QUALITY = 100.0  # bounded CPU sample: same genome and size at quality 100 (1/20 of the iterations)
+# DRAM bytes (read + write) per launch on one full config-1 render, from
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none \
+#       -k "regex:k_iterate|k_de_tile" -c 2 <one config-1 render>   (1 pass)
+ITERATE_TRAFFIC = 26.14e6 + 1.47e6    # k_iterate: bucket atomics resolve in L2
+TAIL_TRAFFIC = 136.54e6 + 3.54e6      # k_de_tile: the histogram once, part of the image
 
 
 def peaks():
@@ -241,12 +246,12 @@ def run_gpu(args):
                    "iterate_ms": 1e3 * it_s / args.steps, "tail_ms": 1e3 * tail_s / args.steps,
                    "wall_ms": 1e3 * wall_s / args.steps, "parallelism": "replicas" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "kernel": "k_iterate", "achieved": it_gbs, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": it_gbs / hbm_peak, "traffic": None,
+                     "unit": "GB/s", "frac": it_gbs / hbm_peak, "traffic": ITERATE_TRAFFIC,
                      "note": f"16 B bucket RMW per plotted sample ({plotted / args.steps / 1e9:.3f} G/render); "
                              f"peak {peak_kind}; the kernel is issue/latency bound, not HBM bound"},
         "roofline_tail": {"bound": "hbm", "kernel": "DE + filter + tonemap", "achieved": tail_gbs,
                           "peak": hbm_peak, "unit": "GB/s",
-                          "frac": (tail_gbs / hbm_peak) if tail_gbs else None, "traffic": None,
+                          "frac": (tail_gbs / hbm_peak) if tail_gbs else None, "traffic": TAIL_TRAFFIC,
                           "note": f"histogram {hist_bytes / 1e6:.1f} MB read + image {out_bytes / 1e6:.1f} MB "
                                   f"write per render; peak {peak_kind}"},
         "e2e": {"value": e2e, "unit": "Giter/s", "h2d_bytes_per_step": int(recs[0][2]["h2d_bytes"]),

@@ -53,7 +53,7 @@ struct DEParams {
 /* sources with more taps than this inside the region go to the shared list
  * (one warp per source); fewer are scattered by the classifying thread */
 #ifndef DE_SMALL_TAPS
-#define DE_SMALL_TAPS 16
+#define DE_SMALL_TAPS 4
 #endif
 
 __device__ __forceinline__ float de_coef(float4 ki, int r2) {

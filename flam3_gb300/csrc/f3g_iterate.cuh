@@ -32,6 +32,12 @@
 
 namespace f3g {
 
+/* F3G_FINAL_UNROLL: 1 gives the final xform its own apply_xform call site
+ * (more code, fewer loop branches); 0 (default) shares one site */
+#ifndef F3G_FINAL_UNROLL
+#define F3G_FINAL_UNROLL 0
+#endif
+
 template <typename R> struct PassS {
   int num_xforms, num_std, final_index, final_enable, chaos_enable, fuse, mode, full;
   int width, height, nbuckets, rotate, cmap_size, palette_mode, bucket_kind, S;
@@ -43,6 +49,9 @@ template <typename R> struct PassS {
   void *buckets, *count;
   uint16_t nbrk[F3G_MAX_XFORMS + 1];
   uint16_t brk[F3G_MAX_XFORMS + 1][F3G_MAX_XFORMS];
+  /* row 0 by the top 8 of the 14 bits: the xform when no breakpoint falls
+   * in the bucket, else 0x8000 | breakpoints below the bucket */
+  uint16_t lut[256];
   uint8_t var_id[F3G_MAX_VARLIST];
   R var_w[F3G_MAX_VARLIST];
   float4 dmap[256];
@@ -79,6 +88,15 @@ __device__ void stage_pass(PassS<R> &s, const F3GPass *__restrict__ p) {
     s.brk[r][c] = p->brk[r][c];
   }
   for (int i = t; i < rows; i += T) s.nbrk[i] = p->nbrk[i];
+  for (int b = t; b < 256; b += T) {
+    const int n = p->nbrk[0];
+    int lo = 0, hi = 0;
+    for (int k = 0; k < n; k++) {
+      lo += p->brk[0][k] <= (uint16_t)(b << 6);
+      hi += p->brk[0][k] <= (uint16_t)((b << 6) | 63);
+    }
+    s.lut[b] = (uint16_t)(lo == hi ? lo : (0x8000 | lo));
+  }
   for (int i = t; i < F3G_MAX_VARLIST; i += T) {
     s.var_id[i] = p->var_id[i];
     s.var_w[i] = (R)p->var_w[i];
@@ -107,25 +125,35 @@ __device__ void stage_pass(PassS<R> &s, const F3GPass *__restrict__ p) {
   }
 }
 
-/* xform choice: the number of breakpoints of row `row` that are <= v */
+/* xform choice: the number of breakpoints of row `row` that are <= v
+ * (row 0 through the 256-entry table, scanning only inside a bucket that
+ * holds a breakpoint) */
 template <typename R>
 __device__ __forceinline__ int pick_xform(const PassS<R> &s, int row, uint32_t v) {
+  if (row == 0) {
+    const int e = s.lut[v >> 6];
+    if (!(e & 0x8000)) return e;
+    int fn = e & 0x7fff;
+    const int n = s.nbrk[0];
+    while (fn < n && s.brk[0][fn] <= v) fn++;
+    return fn;
+  }
   int n = s.nbrk[row], fn = 0;
   for (int k = 0; k < n; k++) fn += (s.brk[row][k] <= v);
   return fn;
 }
 
-/* rect.c:411-516 for one sample */
+/* Bucket of a point (rect.c:411-440): optional rotation about rot_center,
+ * the inclusive bounds test, the index; -1 outside the histogram. */
 template <typename R>
-__device__ __forceinline__ unsigned plot(const PassS<R> &s, R qx, R qy, R qc, R qo) {
+__device__ __forceinline__ int bucket_of(const PassS<R> &s, R qx, R qy) {
   R p0 = qx, p1 = qy;
   if (s.rotate) {
     R p00 = qx - s.rcx, p11 = qy - s.rcy;
     p0 = p00 * s.r00 + p11 * s.r01 + s.rcx;
     p1 = p00 * s.r10 + p11 * s.r11 + s.rcy;
   }
-  if (!(p0 >= s.b0 && p1 >= s.b1 && p0 <= s.b2 && p1 <= s.b3)) return 0u;
-  if (qo == (R)0) return 0u;
+  if (!(p0 >= s.b0 && p1 >= s.b1 && p0 <= s.b2 && p1 <= s.b3)) return -1;
   int xi, yi;
   if (sizeof(R) == 8) {
     xi = (int)(s.dws0 * (double)p0 - s.dwb0s0);
@@ -138,7 +166,18 @@ __device__ __forceinline__ unsigned plot(const PassS<R> &s, R qx, R qy, R qc, R 
   }
   /* inside the bounds xi <= W and yi <= H, so the index fits 32 bits */
   const int idx = xi + s.width * yi;
-  if (idx < 0 || idx >= s.nbuckets) return 0u;
+  return (idx < 0 || idx >= s.nbuckets) ? -1 : idx;
+}
+
+/* rect.c:411-516 for one sample.  With `agg` (warp-uniform), lanes of the
+ * converged group that hit the same bucket are summed through shuffles and
+ * added with one atomic by the lowest such lane: attractors concentrated on
+ * few buckets otherwise serialise on same-address atomics in L2. */
+template <typename R>
+__device__ __forceinline__ unsigned plot(const PassS<R> &s, R qx, R qy, R qc, R qo, bool agg = false) {
+  const int idx = bucket_of(s, qx, qy);
+  if (idx < 0) return 0u;
+  if (qo == (R)0) return 0u;
   float4 col;
   const R dbl_index0 = qc * (R)s.cmap_size;
   int ci = (int)dbl_index0;
@@ -161,6 +200,25 @@ __device__ __forceinline__ unsigned plot(const PassS<R> &s, R qx, R qy, R qc, R 
     float o = (float)qo;
     col.x *= o; col.y *= o; col.z *= o; col.w *= o;
     cnt *= o;
+  }
+  if (agg) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, idx);
+    if (peers != (1u << (threadIdx.x & 31))) {
+      float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+      float csum = 0.f;
+      for (unsigned m = peers; m; m &= m - 1) {
+        const int src = __ffs(m) - 1;
+        sum.x += __shfl_sync(peers, col.x, src);
+        sum.y += __shfl_sync(peers, col.y, src);
+        sum.z += __shfl_sync(peers, col.z, src);
+        sum.w += __shfl_sync(peers, col.w, src);
+        csum += __shfl_sync(peers, cnt, src);
+      }
+      if ((int)(threadIdx.x & 31) != __ffs(peers) - 1) return 1u;
+      col = sum;
+      cnt = csum;
+    }
   }
   if (s.bucket_kind == F3G_BK_F32) {
     float4 *b = (float4 *)s.buckets + idx;
@@ -186,7 +244,11 @@ __device__ __forceinline__ bool chain_step(const PassS<R> &s, int fn, R &px, R &
                                            int &lastxf, unsigned &bad, R &qx, R &qy, R &qc, R &qo, G &rng) {
   int cur = fn;
   R ix = px, iy = py, ic = pc;
+#if F3G_FINAL_UNROLL
+#pragma unroll
+#else
 #pragma unroll 1
+#endif
   for (int stage = 0; stage < 2; stage++) {
     R nx, ny, nc, no;
     const bool b = apply_xform<R, FULL, G>(s.xf[cur], s.var_id, s.var_w, ix, iy, ic, nx, ny, nc, no, rng);
@@ -243,6 +305,20 @@ __device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, int S
   bad_total += bad;
 }
 
+/* F3G_AGG: 0 never aggregate bucket adds, 1 (default) always for FP64
+ * buckets (four atomics per sample) and, for FP32 buckets, per chunk when
+ * probes find at least F3G_AGG_LANES of a warp's points sharing buckets,
+ * 2 always.  Measured on the config-1 still / a config-2 key genome whose
+ * attractor covers few buckets: never 45.9 / 10.0 Giter/s, 8 lanes 41.3 /
+ * 38.1, 16 lanes 44.1 / 38.2, always 38.0 / 41.0; FP64 buckets 13.9
+ * without, 20.2 with aggregation. */
+#ifndef F3G_AGG
+#define F3G_AGG 1
+#endif
+#ifndef F3G_AGG_LANES
+#define F3G_AGG_LANES 16
+#endif
+
 /* Warp-shared stream of xform-choice words: lane L holds words 4L..4L+3 of
  * the current 128-word block of counter (chunk, block, 0xC0DE0000 | warp,
  * L), so one Philox call per lane serves 128 steps of the warp; word k is
@@ -292,6 +368,12 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
   int fuse_left = s.fuse;
   long long remaining = q;
   uint32_t rot = 0;
+  /* warp-aggregated accumulation: always for FP64 buckets; for FP32 it is
+   * switched on for the rest of the chunk when probes (rounds 7, 15, 23, 31,
+   * warp converged) find many of the warp's points sharing buckets in two of
+   * four probes */
+  bool agg = F3G_AGG == 2 || (F3G_AGG == 1 && s.bucket_kind == F3G_BK_F64);
+  int probes = 0, dups = 0;
   for (int round = 0;; round++) {
     for (int k = 0; k < shuffle_every; k++) {
       const uint32_t w = ww.word();
@@ -301,11 +383,21 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
       if (ok) {
         if (fuse_left > 0) fuse_left--;
         else if (remaining > 0) {
-          hits += plot(s, qx, qy, qc, qo);
+          hits += plot(s, qx, qy, qc, qo, agg);
           remaining--;
         }
       }
     }
+#if F3G_AGG == 1
+    if (!agg && probes < 4 && (round & 7) == 7) {
+      __syncwarp();
+      const int b = bucket_of(s, px, py);
+      const unsigned peers = __match_any_sync(0xffffffffu, b < 0 ? -1 - lane : b);
+      const unsigned shared = __ballot_sync(0xffffffffu, __popc(peers) > 1);
+      dups += __popc(shared) >= F3G_AGG_LANES;
+      if (++probes == 4) agg = dups >= 2;
+    }
+#endif
     rot += 0x9E3779B1u * (uint32_t)(round + 1);
     /* transpose lanes across warps, XOR the low five bits and rotate by
      * whole 32-point segments (block-uniform amounts); points are stored
@@ -451,8 +543,9 @@ static __global__ void __launch_bounds__(256) k_accumulate(const F3GPass *__rest
   PassS<double> &s = *reinterpret_cast<PassS<double> *>(smem_raw);
   stage_pass<double>(s, pass);
   __syncthreads();
+  /* warp-aggregated accumulation, so the parity tests cover the shuffle sums */
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-    (void)plot<double>(s, pts[4 * k], pts[4 * k + 1], pts[4 * k + 2], pts[4 * k + 3]);
+    (void)plot<double>(s, pts[4 * k], pts[4 * k + 1], pts[4 * k + 2], pts[4 * k + 3], true);
 }
 
 template <typename R, bool FULL>

@@ -63,3 +63,23 @@ def test_accumulate_matches_oracle(gpulib, palette_mode):
     # colours are staged as FP32 on the device: equal to FP32 rounding
     np.testing.assert_allclose(hg, ho, rtol=2e-6, atol=1e-3)
     assert ho[..., 4].sum() > 0
+
+
+def test_accumulate_concentrated_points_match_oracle(gpulib):
+    """Most points of a warp land in a handful of buckets: the warp-aggregated
+    sums (shuffle reductions, one atomic per bucket) equal the oracle's
+    one-by-one adds to FP32 rounding."""
+    G = gm.config0_genome(2)
+    gm.resize(G, 32, 24)
+    F = gm.Frame(G)
+    rng = np.random.default_rng(5)
+    n = 100000
+    centers = rng.normal(0.0, 0.3, (5, 2)) + np.array([G.g.center[0], G.g.center[1]])
+    pick = rng.integers(0, 5, n)
+    pts = np.stack([centers[pick, 0] + rng.normal(0, 1e-4, n), centers[pick, 1] + rng.normal(0, 1e-4, n),
+                    rng.uniform(0, 1, n), rng.choice([1.0, 0.5], n)], 1)
+    ho = _oracle.oracle_accumulate(F, pts)
+    hg = render.accumulate_points(F, pts)
+    np.testing.assert_allclose(hg, ho, rtol=2e-6, atol=1e-3)
+    assert (ho[..., 4] > 0).sum() <= 20
+
