@@ -168,6 +168,20 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def combine_ranks(dev_s, wall_s, iters, world, device="cuda"):
+    """Replicas: the timed spans are the maximum over ranks, the work is the
+    sum of every rank's renders (each rank renders the same workload)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([dev_s, wall_s], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, wall_s = float(t[0]), float(t[1])
+        iters *= world
+    return dev_s, wall_s, iters
+
+
 def flush_l2(buf):
     import torch
 
@@ -219,11 +233,7 @@ def run_gpu(args):
     wall_s = sum(r[1] for r in recs)
     it_s = sum(r[2]["iterate_ms"] / 1e3 for r in recs)
     tail_s = sum((r[2]["de_ms"] + r[2]["tail_ms"]) / 1e3 for r in recs)
-    if world > 1:
-        t = torch.tensor([dev_s, wall_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s, wall_s = float(t[0]), float(t[1])
-        iters *= world
+    dev_s, wall_s, iters = combine_ranks(dev_s, wall_s, iters, world)
     if rank != 0:
         return
     plotted = sum(r[2]["plotted"] for r in recs)
