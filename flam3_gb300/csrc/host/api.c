@@ -201,3 +201,125 @@ int flam3gpu_accumulate_points(flam3_frame *f, int field, const double *points, 
   f3g_clear_error();
   return f3g_accumulate_impl(f, field, points, n, hist, hist_w, hist_h);
 }
+
+/* ---- callers of flam3_iterate (flam3.c:351-391, 3574-3640) on the GPU ----
+ * Both draw their chains from the chain kernel (FP32 iteration, fuse 20 as
+ * the reference); the start points and the Philox key come from the
+ * caller's ISAAC context, which advances by 2 words per chain plus 2. */
+
+/* flam3_random_isaac_11 (flam3.c:2523-2525) */
+static double isaac_11(randctx *rc) { return (((int)f3g_irand(rc) & 0xfffffff) - 0x7ffffff) / (double)0x7ffffff; }
+
+static int chains_from_rc(flam3_genome *cp, int nchains, int n, randctx *rc, double *samples, long *bad) {
+  double *starts = (double *)malloc((size_t)(nchains > 0 ? nchains : 1) * 4 * sizeof(double));
+  if (!starts) {
+    f3g_set_error("host memory exhausted");
+    return 1;
+  }
+  for (int c = 0; c < nchains; c++) {
+    starts[4 * c] = isaac_11(rc);
+    starts[4 * c + 1] = isaac_11(rc);
+    starts[4 * c + 2] = 0.0;
+    starts[4 * c + 3] = 0.0;
+  }
+  const uint64_t seed = (uint64_t)(uint32_t)f3g_irand(rc) | ((uint64_t)(uint32_t)f3g_irand(rc) << 32);
+  int r = flam3gpu_iterate_chains(cp, nchains, n, 20, starts, seed, samples, bad, 32);
+  free(starts);
+  return r;
+}
+
+/* k-th smallest of v[0..n) (Hoare's selection), v reordered */
+static double select_kth(double *v, long n, long k) {
+  long lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const double piv = v[lo + (hi - lo) / 2];
+    long i = lo, j = hi;
+    while (i <= j) {
+      while (v[i] < piv) i++;
+      while (v[j] > piv) j--;
+      if (i <= j) {
+        const double t = v[i];
+        v[i] = v[j];
+        v[j] = t;
+        i++;
+        j--;
+      }
+    }
+    if (k <= j) hi = j;
+    else if (k >= i) lo = i;
+    else return v[k];
+  }
+  return v[k];
+}
+
+int flam3gpu_estimate_bounding_box(flam3_genome *cp, double eps, int nsamples, double *bmin, double *bmax,
+                                   randctx *rc) {
+  f3g_clear_error();
+  if (nsamples <= 0) nsamples = 10000;
+  const int per = 1024;
+  const int nchains = (nsamples + per - 1) / per;
+  const int n = (nsamples + nchains - 1) / nchains;
+  const long total = (long)nchains * n;
+  double *pts = (double *)malloc((size_t)total * 4 * sizeof(double));
+  double *axis = (double *)malloc((size_t)total * sizeof(double));
+  long bv = 0;
+  int ret = -1;
+  if (!pts || !axis) {
+    f3g_set_error("host memory exhausted");
+    goto out;
+  }
+  if (chains_from_rc(cp, nchains, n, rc, pts, &bv)) goto out;
+  /* flam3.c:3601-3639 */
+  if (bv / (double)total > eps) eps = 3 * bv / (double)total;
+  if (eps > 0.3) eps = 0.3;
+  const long low = (long)(total * eps), high = total - low;
+  for (int d = 0; d < 2; d++) {
+    if (low == 0) {
+      double mn = 1e10, mx = -1e10;
+      for (long i = 0; i < total; i++) {
+        const double x = pts[4 * i + d];
+        if (x < mn) mn = x;
+        if (x > mx) mx = x;
+      }
+      bmin[d] = mn;
+      bmax[d] = mx;
+    } else {
+      for (long i = 0; i < total; i++) axis[i] = pts[4 * i + d];
+      bmin[d] = select_kth(axis, total, low);
+      bmax[d] = select_kth(axis, total, high);
+    }
+  }
+  ret = (int)bv;
+out:
+  free(pts);
+  free(axis);
+  return ret;
+}
+
+int flam3gpu_colorhist(flam3_genome *cp, int num_batches, randctx *rc, double *hist) {
+  f3g_clear_error();
+  const int sbs = 10000;
+  memset(hist, 0, 256 * sizeof(double));
+  if (num_batches <= 0) return 0;
+  double *pts = (double *)malloc((size_t)num_batches * sbs * 4 * sizeof(double));
+  if (!pts) {
+    f3g_set_error("host memory exhausted");
+    return 1;
+  }
+  long bv = 0;
+  if (chains_from_rc(cp, num_batches, sbs, rc, pts, &bv)) {
+    free(pts);
+    return 1;
+  }
+  const long total = (long)num_batches * sbs;
+  for (long i = 0; i < total; i++) {
+    int c = (int)(pts[4 * i + 2] * 256);
+    if (c < 0) c = 0;
+    if (c > 255) c = 255;
+    hist[c] += 1;
+  }
+  for (int k = 0; k < 256; k++) hist[k] /= (float)total;
+  free(pts);
+  return 0;
+}
+

@@ -46,6 +46,7 @@ int f3g_build_batch_passes(flam3_frame *spec, int field, const f3g_geom *g, int 
 int f3g_camera(flam3_frame *spec, const flam3_genome *cp, int field, const f3g_geom *g, F3GPass *p,
                double *sample_density, double *ppux, double *ppuy);
 void f3g_pass_key(flam3_frame *spec, uint32_t key[2]);
+unsigned long f3g_irand(randctx *r);
 
 /* error reporting: message kept per thread, also printed to stderr */
 void f3g_set_error(const char *fmt, ...);

@@ -928,3 +928,8 @@ int f3g_camera(flam3_frame *spec, const flam3_genome *cp, int field, const f3g_g
 }
 
 void f3g_pass_key(flam3_frame *spec, uint32_t key[2]) { consume_rc(spec, key); }
+
+/* the ISAAC word stream of a caller's context (isaac.h:49-52), for host
+ * entry points that draw from it */
+unsigned long f3g_irand(randctx *r) { return irand(r); }
+

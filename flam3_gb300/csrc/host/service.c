@@ -43,7 +43,7 @@
 #define NTAIL 8       /* tail slots */
 #define NBRANCH 4     /* parallel branches of a tail graph */
 #define NCLASS 4      /* kernel classes: full variations x xform-choice mode */
-#define NGRAPH 8      /* cached executable tail graphs */
+#define NGRAPH 32     /* cached executable tail graphs */
 
 enum { J_QUEUED = 0, J_ACTIVE, J_DONE, J_FAILED };
 enum { P_ITER = 0, P_TAIL, P_WAIT_UP };
@@ -903,7 +903,28 @@ static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n) {
   for (int k = 0; k < s->cfg.streams; k++) cudaStreamWaitEvent(s->s_tail, s->ev_last[k], 0);
   cudaEventRecord(t->t0, s->s_tail);
   int err = 0;
-  if (s->cfg.tail_graphs) {
+  if (s->cfg.tail_graphs == 1) {
+    /* one graph per job tail, keyed by its shape; the executable graph of a
+     * shape is updated in place with the next job's buffers and sizes */
+    for (int i = 0; i < n && !err; i++) {
+      char sig[128];
+      sig[0] = 0;
+      cudaGraph_t graph = NULL;
+      if (cudaStreamBeginCapture(s->s_tail, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        err = 1;
+        break;
+      }
+      err = enqueue_tail_ops(s, jobs[i], s->s_tail, sig, sizeof(sig));
+      if (cudaStreamEndCapture(s->s_tail, &graph) != cudaSuccess) err = 1;
+      if (!err) {
+        cudaGraphExec_t ex = graph_for(s, graph, sig);
+        if (!ex || cudaGraphLaunch(ex, s->s_tail) != cudaSuccess) err = 1;
+        s->c_graphs++;
+      }
+      if (graph) cudaGraphDestroy(graph);
+    }
+  } else if (s->cfg.tail_graphs == 2) {
+    /* one graph per round, one branch per job across tail_branches streams */
     char sig[512];
     sig[0] = 0;
     cudaGraph_t graph = NULL;

@@ -64,6 +64,8 @@ def load():
     lib.flam3gpu_iterate_chains.argtypes = [G, C.c_int, C.c_int, C.c_int, dp, C.c_uint64, dp,
                                             C.POINTER(C.c_long), C.c_int]
     lib.flam3gpu_interpolate.argtypes = [G, C.c_int, C.c_double, C.c_double, G]
+    lib.flam3gpu_estimate_bounding_box.argtypes = [G, C.c_double, C.c_int, dp, dp, C.POINTER(abi.randctx)]
+    lib.flam3gpu_colorhist.argtypes = [G, C.c_int, C.POINTER(abi.randctx), dp]
     lib.flam3gpu_free_genome.argtypes = [G]
     lib.flam3gpu_free_genome.restype = None
     lib.flam3gpu_set_interpolator.argtypes = [C.c_void_p]
@@ -218,4 +220,34 @@ def interpolate(genomes, time, stagger=0.0):
     if lib.flam3gpu_interpolate(arr, len(structs), float(time), float(stagger), C.byref(out)):
         _err(lib, "flam3gpu_interpolate")
     return InterpolatedGenome(out)
+
+
+def estimate_bounding_box(genome, eps=0.01, nsamples=10000, rc=None):
+    """flam3_estimate_bounding_box on the GPU: (bmin, bmax, bad values)."""
+    lib = load()
+    from .isaac import init_rc
+    if rc is None:
+        rc = abi.randctx()
+        init_rc(rc, b"bbox")
+    bmin = np.zeros(2)
+    bmax = np.zeros(2)
+    g = getattr(genome, "g", genome)
+    bv = lib.flam3gpu_estimate_bounding_box(C.byref(g), eps, nsamples, _dptr(bmin), _dptr(bmax), C.byref(rc))
+    if bv < 0:
+        _err(lib, "flam3gpu_estimate_bounding_box")
+    return bmin, bmax, bv
+
+
+def colorhist(genome, num_batches=10, rc=None):
+    """flam3_colorhist on the GPU: 256 normalised bins."""
+    lib = load()
+    from .isaac import init_rc
+    if rc is None:
+        rc = abi.randctx()
+        init_rc(rc, b"colorhist")
+    hist = np.zeros(256)
+    g = getattr(genome, "g", genome)
+    if lib.flam3gpu_colorhist(C.byref(g), num_batches, C.byref(rc), _dptr(hist)):
+        _err(lib, "flam3gpu_colorhist")
+    return hist
 

@@ -66,6 +66,20 @@ int flam3gpu_iterate_chains(flam3_genome *cp, int nchains, int n, int fuse,
                             const double *starts, uint64_t seed, double *samples,
                             long *badvals, int precision);
 
+/* flam3_estimate_bounding_box (flam3.h:588, flam3.c:3574-3640) on the GPU: same
+ * arguments, eps rule and return value (bad values met, -1 on failure); the
+ * nsamples points come from chains of 1024 samples after 20 fuse steps
+ * (the reference: one chain) drawn with the counter-based stream, so the box
+ * matches the reference's statistically, not bit for bit.  Start points and
+ * the stream key are drawn from rc. */
+int flam3gpu_estimate_bounding_box(flam3_genome *cp, double eps, int nsamples, double *bmin, double *bmax,
+                                   randctx *rc);
+
+/* flam3_colorhist (flam3.h:587, flam3.c:351-391) on the GPU: hist[256] is the
+ * normalised histogram of the colour coordinate over num_batches chains of
+ * 10000 samples after 20 fuse steps.  Returns 0 on success. */
+int flam3gpu_colorhist(flam3_genome *cp, int num_batches, randctx *rc, double *hist);
+
 /* flam3gpu_render without device allocation.  No counterpart in the
  * reference: for callers that cannot call cudaMalloc (inside CUDA-graph
  * construction, under a host-owned memory pool, with a fixed device-memory

@@ -14,8 +14,8 @@
  *     temporal samples (per-job work lists in one chunk queue), shortest
  *     remaining job first; rounds may alternate over several streams;
  *   - jobs whose iteration finished in a round get their density
- *     estimation / filter / tonemap / copy-out in one CUDA graph per round,
- *     updated in place when a later round's tail has the same shape;
+ *     estimation / filter / tonemap / copy-out as CUDA graphs: one
+ *     executable graph per tail shape, updated in place for each job;
  *   - requests that arrive while others run join at the next round
  *     (continuous batching); histograms, pass tables and chunk cursors stay
  *     resident on the device between rounds.
@@ -46,12 +46,14 @@ typedef struct {
   long long round_samples;  /* samples per iterate round (0: automatic -- at least 2e8 samples and
                                4 chunks per resident block; -1: one round holds all admitted work) */
   int max_active;           /* admitted jobs at once (0: unlimited) */
-  int tail_graphs;          /* 1: per-round tail in a CUDA graph (default); 0: direct launches */
+  int tail_graphs;          /* 1 (default): each job's tail is a CUDA graph per tail shape, updated in
+                               place for the next job of that shape; 2: one graph per round with
+                               tail_branches parallel branches; 0: direct launches */
   int streams;              /* iterate streams rounds alternate over (default 1; with 2 the next
                                round's blocks fill the SMs a draining round frees) */
   int use_tuning;           /* 1: apply the autotuned table (flam3gpu_autotune) to new jobs */
   int max_inflight;         /* iterate rounds queued on the device at once (default 2) */
-  int tail_branches;        /* parallel branches of a round's tail graph (default 1: one chain) */
+  int tail_branches;        /* parallel branches of a round's tail graph with tail_graphs 2 (default 1) */
   int reserved[6];
 } flam3gpu_service_config;
 

@@ -83,3 +83,54 @@ def test_accumulate_concentrated_points_match_oracle(gpulib):
     np.testing.assert_allclose(hg, ho, rtol=2e-6, atol=1e-3)
     assert (ho[..., 4] > 0).sum() <= 20
 
+
+
+def _rc_chain_inputs(seed, nchains):
+    """The start points and stream key flam3gpu_colorhist / _bounding_box
+    draw from a caller's ISAAC context (flam3.c:2523-2525 for the starts)."""
+    from flam3_gb300 import abi as _abi
+    from flam3_gb300.isaac import init_rc, irand
+
+    rc = _abi.randctx()
+    init_rc(rc, seed)
+    u = lambda: (((irand(rc) & 0xfffffff) - 0x7ffffff) / float(0x7ffffff))
+    starts = np.array([[u(), u(), 0.0, 0.0] for _ in range(nchains)])
+    key = irand(rc) & 0xffffffff
+    key |= (irand(rc) & 0xffffffff) << 32
+    return starts, key
+
+
+def test_bounding_box_matches_oracle_chains(gpulib):
+    from flam3_gb300 import abi as _abi
+    from flam3_gb300.isaac import init_rc
+
+    G = gm.config1_genome(1, width=320, height=180, quality=10.0)
+    nsamples, per = 200 * 1024, 1024
+    rc = _abi.randctx()
+    init_rc(rc, b"bb")
+    bmin, bmax, bv = render.estimate_bounding_box(G, 0.01, nsamples, rc)
+    starts, key = _rc_chain_inputs(b"bb", nsamples // per)
+    pts = _oracle.oracle_iterate_chains(G, starts, per, 20, key)[0].reshape(-1, 4)
+    lo = np.quantile(pts[:, :2], 0.01, axis=0)
+    hi = np.quantile(pts[:, :2], 0.99, axis=0)
+    span = hi - lo
+    # FP32 chains decorrelate from the FP64 oracle's after tens of steps:
+    # the same distribution, so the quantiles agree to sampling noise
+    assert np.all(np.abs(bmin - lo) < 0.03 * span), (bmin, lo)
+    assert np.all(np.abs(bmax - hi) < 0.03 * span), (bmax, hi)
+    assert bv == 0
+
+
+def test_colorhist_matches_oracle_chains(gpulib):
+    from flam3_gb300 import abi as _abi
+    from flam3_gb300.isaac import init_rc
+
+    G = gm.config1_genome(2, width=320, height=180, quality=10.0)
+    rc = _abi.randctx()
+    init_rc(rc, b"ch")
+    h = render.colorhist(G, 20, rc)
+    starts, key = _rc_chain_inputs(b"ch", 20)
+    pts = _oracle.oracle_iterate_chains(G, starts, 10000, 20, key)[0].reshape(-1, 4)
+    ho = np.bincount(np.clip((pts[:, 2] * 256).astype(int), 0, 255), minlength=256) / len(pts)
+    assert abs(h.sum() - 1.0) < 1e-6
+    assert np.abs(h - ho).sum() < 0.08, np.abs(h - ho).sum()

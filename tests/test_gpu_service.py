@@ -139,18 +139,22 @@ def test_render_batch_equals_plain(gpulib):
 
 def test_tail_graphs_and_direct_tails_agree(gpulib):
     outs = []
-    for graphs in (1, 0):
-        with service.Service(tail_graphs=graphs) as svc:
-            ts = [svc.submit(frame(k, 0), nchan=NCHAN.get(k, 3)) for k in KINDS]
+    for graphs, branches in ((1, 1), (2, 3), (0, 1)):
+        with service.Service(tail_graphs=graphs, tail_branches=branches) as svc:
+            ts = [svc.submit(frame(k, 0), nchan=NCHAN.get(k, 3)) for k in KINDS + KINDS]
             outs.append([svc.wait(t)[0] for t in ts])
             cnt = svc.counters()
         if graphs:
             assert cnt["tail_graphs"] >= 1
         else:
             assert cnt["tail_graphs"] == 0
-    for a, b in zip(*outs):
-        ok, info = close_images(a, b)
-        assert ok, info
+        if graphs == 1:
+            # one executable graph per tail shape, reused for the repeats
+            assert cnt["graphs_instantiated"] < len(KINDS) * 2
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            ok, info = close_images(a, b)
+            assert ok, info
 
 
 def test_admission_by_budget(gpulib):
