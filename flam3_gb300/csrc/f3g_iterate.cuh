@@ -308,16 +308,17 @@ __device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, int S
 
 /* F3G_AGG: 0 never aggregate bucket adds, 1 (default) always for FP64
  * buckets (four atomics per sample) and, for FP32 buckets, per chunk when
- * probes find at least F3G_AGG_LANES of a warp's points sharing buckets,
- * 2 always.  Measured on the config-1 still / a config-2 key genome whose
- * attractor covers few buckets: never 45.9 / 10.0 Giter/s, 8 lanes 41.3 /
- * 38.1, 16 lanes 44.1 / 38.2, always 38.0 / 41.0; FP64 buckets 13.9
- * without, 20.2 with aggregation. */
+ * probes taken right after block shuffles find at least F3G_AGG_LANES of a
+ * warp's points sharing buckets, 2 always.  Measured on the config-1 still /
+ * a config-2 key genome whose attractor covers few buckets: never 45.9 /
+ * 10.0 Giter/s, always 38.0 / 41.0, probed after the shuffle with 8 lanes
+ * 48.7 / 39.2 (the config-1 chunks stay direct); FP64 buckets 13.9 without,
+ * 20.2 with aggregation. */
 #ifndef F3G_AGG
 #define F3G_AGG 1
 #endif
 #ifndef F3G_AGG_LANES
-#define F3G_AGG_LANES 16
+#define F3G_AGG_LANES 8
 #endif
 
 /* Warp-shared stream of xform-choice words: lane L holds words 4L..4L+3 of
@@ -370,9 +371,9 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
   long long remaining = q;
   uint32_t rot = 0;
   /* warp-aggregated accumulation: always for FP64 buckets; for FP32 it is
-   * switched on for the rest of the chunk when probes (rounds 7, 15, 23, 31,
-   * warp converged) find many of the warp's points sharing buckets in two of
-   * four probes */
+   * switched on for the rest of the chunk when probes (after the shuffles of
+   * rounds 7, 15, 23, 31) find many of the warp's points sharing buckets in
+   * two of four probes */
   bool agg = F3G_AGG == 2 || (F3G_AGG == 1 && s.bucket_kind == F3G_BK_F64);
   int probes = 0, dups = 0;
   for (int round = 0;; round++) {
@@ -389,16 +390,7 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
         }
       }
     }
-#if F3G_AGG == 1
-    if (!agg && probes < 4 && (round & 7) == 7) {
-      __syncwarp();
-      const int b = bucket_of(s, px, py);
-      const unsigned peers = __match_any_sync(0xffffffffu, b < 0 ? -1 - lane : b);
-      const unsigned shared = __ballot_sync(0xffffffffu, __popc(peers) > 1);
-      dups += __popc(shared) >= F3G_AGG_LANES;
-      if (++probes == 4) agg = dups >= 2;
-    }
-#endif
+
     rot += 0x9E3779B1u * (uint32_t)(round + 1);
     /* transpose lanes across warps, XOR the low five bits and rotate by
      * whole 32-point segments (block-uniform amounts); points are stored
@@ -412,6 +404,18 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
     int more = __syncthreads_or(remaining > 0 || fuse_left > 0);
     px = bx[rslot]; py = by[rslot]; pc = bc[rslot]; consec = bq[rslot];
     if (!more) break;
+#if F3G_AGG == 1
+    /* probe right after the shuffle (block converged), when a warp holds
+     * points from every warp: shared buckets then reflect the attractor,
+     * not the steps the warp's lanes took together */
+    if (!agg && probes < 4 && (round & 7) == 7) {
+      const int b = bucket_of(s, px, py);
+      const unsigned peers = __match_any_sync(0xffffffffu, b < 0 ? -1 - lane : b);
+      const unsigned shared = __ballot_sync(0xffffffffu, __popc(peers) > 1);
+      dups += __popc(shared) >= F3G_AGG_LANES;
+      if (++probes == 4) agg = dups >= 2;
+    }
+#endif
   }
   (void)po;
   bad_total += bad;

@@ -26,13 +26,13 @@ const char *flam3gpu_last_error(void) { return err_buf; }
 
 const char *flam3gpu_version(void) { return "flam3-gb300 0.1 (sm_103a)"; }
 
-flam3gpu_options f3g_opts = {1, 32, 2, 256, 0, 0, 0, 0, {0}};
+flam3gpu_options f3g_opts = {1, 32, 3, 256, 0, 0, 0, 0, {0}};
 
 void flam3gpu_default_options(flam3gpu_options *o) {
   memset(o, 0, sizeof(*o));
   o->iter_mode = 1;
   o->iter_precision = 32;
-  o->shuffle_every = 2;
+  o->shuffle_every = 3;
   o->threads_per_block = 256;
 }
 
