@@ -11,8 +11,10 @@
  *      kernel), whose counts (+ss border, for the density sums) are staged in
  *      shared memory;
  *   3. every non-empty source whose kernel square meets the region scatters
- *      its taps into the shared accumulator (shared-memory atomics); sources
- *      with many taps are queued and spread over the 32 lanes of a warp;
+ *      its taps into the shared accumulator (shared-memory atomics): sources
+ *      with few taps from their own thread, then, in a second pass in which
+ *      each warp re-classifies 32 sources at a time, each source with many
+ *      taps over the warp's 32 lanes;
  *   4. the filter + tonemap + pack of the tile's pixels read the shared
  *      accumulator; nothing but the image is written to global memory.
  *
@@ -60,6 +62,40 @@ __device__ __forceinline__ float de_coef(float4 ki, int r2) {
   return (float)r2 <= ki.z ? ki.x * exp2f(ki.y * (float)r2) : 0.0f;
 }
 
+/* Classifies source k of the tile's S x S source window (rect.c:79-117):
+ * returns false when it adds nothing to the region, else its kernel, its
+ * clipped tap rectangle inside the region and its bucket coordinates. */
+struct DESource {
+  int sx, sy, fi, x_lo, x_hi, y_lo, y_hi;
+};
+
+__device__ __forceinline__ bool de_classify(const DEParams &P, const float *cnt, const float4 *kin, int k, int S,
+                                            int Cc, int ax0, int ay0, int A, int R, int ss, int istart, int iend,
+                                            int jstart, int jend, DESource &o) {
+  const int lx = k % S, ly = k / S;
+  const int sx = ax0 - R + lx, sy = ay0 - R + ly;
+  if (sx < istart || sx >= iend || sy < jstart || sy >= jend) return false;
+  if (cnt[(lx + ss) + (ly + ss) * Cc] == 0.0f) return false;
+  float f = 0.0f;
+  for (int jj = -ss; jj <= ss; jj++)
+    for (int ii = -ss; ii <= ss; ii++) f += cnt[(lx + ss + ii) + (ly + ss + jj) * Cc];
+  if (P.scf) f *= P.scfact;
+  int fi;
+  if (f > (float)P.mfc) fi = P.mfi;
+  else if (f <= 100.0f) fi = (int)ceilf(f) - 1;
+  else fi = 100 + (int)floorf(powf(f - 100.0f, P.curve));
+  fi = min(max(fi, 0), P.mfi);
+  const int reach = (int)kin[fi].w;
+  o.sx = sx;
+  o.sy = sy;
+  o.fi = fi;
+  o.x_lo = max(sx - reach, ax0);
+  o.x_hi = min(sx + reach, ax0 + A - 1);
+  o.y_lo = max(sy - reach, ay0);
+  o.y_hi = min(sy + reach, ay0 + A - 1);
+  return o.x_lo <= o.x_hi && o.y_lo <= o.y_hi;
+}
+
 template <bool FUSED>
 __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -70,8 +106,6 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
   float *acc = (float *)(kin + nk);               /* 4 planes of A*A */
   float *cnt = acc + 4 * AA;                      /* Cc*Cc counts / 255 */
   float *filt = cnt + Cc * Cc;                    /* fw*fw (fused) */
-  uint32_t *list = (uint32_t *)(filt + P.fw * P.fw); /* wide sources: local index << 16 | kernel */
-  __shared__ int nlist;
   const int tid = threadIdx.x, nt = blockDim.x;
   int ax0, ay0;
   if (FUSED) {
@@ -82,7 +116,6 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
     ay0 = blockIdx.y * A;
   }
   const int cx0 = ax0 - R - ss, cy0 = ay0 - R - ss;
-  if (tid == 0) nlist = 0;
   for (int k = tid; k < nk; k += nt) kin[k] = P.kinfo[k];
   for (int k = tid; k < 4 * AA; k += nt) acc[k] = 0.0f;
   if (FUSED)
@@ -98,84 +131,74 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
   /* DE loop bounds of the reference (rect.c:79-80, 979) */
   const int istart = P.os - 1, iend = P.W - (P.os - 1);
   const int jstart = P.os - 1, jend = min(P.H, (P.os - 1) + (P.H - 2 * (P.os - 1) + 1));
-  /* 1. classify sources; small ones scatter here (shared atomics) */
+  /* 1. sources with few taps in the region scatter from their thread
+   *    (shared-memory atomics) */
   for (int k = tid; k < S * S; k += nt) {
-    const int lx = k % S, ly = k / S;
-    const int sx = ax0 - R + lx, sy = ay0 - R + ly;
-    if (sx < istart || sx >= iend || sy < jstart || sy >= jend) continue;
-    if (cnt[(lx + ss) + (ly + ss) * Cc] == 0.0f) continue;
-    float f = 0.0f;
-    for (int jj = -ss; jj <= ss; jj++)
-      for (int ii = -ss; ii <= ss; ii++) f += cnt[(lx + ss + ii) + (ly + ss + jj) * Cc];
-    if (P.scf) f *= P.scfact;
-    int fi;
-    if (f > (float)P.mfc) fi = P.mfi;
-    else if (f <= 100.0f) fi = (int)ceilf(f) - 1;
-    else fi = 100 + (int)floorf(powf(f - 100.0f, P.curve));
-    fi = min(max(fi, 0), P.mfi);
-    const float4 ki = kin[fi];
-    const int reach = (int)ki.w;
-    const int x_lo = max(sx - reach, ax0), x_hi = min(sx + reach, ax0 + A - 1);
-    const int y_lo = max(sy - reach, ay0), y_hi = min(sy + reach, ay0 + A - 1);
-    if (x_lo > x_hi || y_lo > y_hi) continue;
-    if ((x_hi - x_lo + 1) * (y_hi - y_lo + 1) > DE_SMALL_TAPS) {
-      list[atomicAdd(&nlist, 1)] = ((uint32_t)k << 16) | (uint32_t)fi;
-      continue;
-    }
-    float4 v = load_bucket(P.buckets, P.bkind, (long long)sx + (long long)sy * P.W);
+    DESource o;
+    if (!de_classify(P, cnt, kin, k, S, Cc, ax0, ay0, A, R, ss, istart, iend, jstart, jend, o)) continue;
+    if ((o.x_hi - o.x_lo + 1) * (o.y_hi - o.y_lo + 1) > DE_SMALL_TAPS) continue;
+    float4 v = load_bucket(P.buckets, P.bkind, (long long)o.sx + (long long)o.sy * P.W);
     if (v.w == 0.0f) continue;
     const float ls = P.k1 * log1pf(v.w * P.k2) / v.w;
     v = make_float4(v.x * ls, v.y * ls, v.z * ls, v.w * ls);
-    for (int y = y_lo; y <= y_hi; y++) {
-      const int dy = y - sy;
-      for (int x = x_lo; x <= x_hi; x++) {
-        const int dx = x - sx;
+    const float4 ki = kin[o.fi];
+    for (int y = o.y_lo; y <= o.y_hi; y++) {
+      const int dy = y - o.sy;
+      for (int x = o.x_lo; x <= o.x_hi; x++) {
+        const int dx = x - o.sx;
         const float w = de_coef(ki, dx * dx + dy * dy);
         if (w == 0.0f) continue;
-        const int o = (x - ax0) + (y - ay0) * A;
-        atomicAdd(acc + o, w * v.x);
-        atomicAdd(acc + AA + o, w * v.y);
-        atomicAdd(acc + 2 * AA + o, w * v.z);
-        atomicAdd(acc + 3 * AA + o, w * v.w);
+        const int off = (x - ax0) + (y - ay0) * A;
+        atomicAdd(acc + off, w * v.x);
+        atomicAdd(acc + AA + off, w * v.y);
+        atomicAdd(acc + 2 * AA + off, w * v.z);
+        atomicAdd(acc + 3 * AA + off, w * v.w);
       }
     }
   }
-  __syncthreads();
-  /* 2. wide sources: one warp per source, lanes over its taps inside the
-   * region (row-major; each lane advances by 32 taps without dividing) */
-  const int nl = nlist;
+  /* 2. sources with many taps: each warp classifies 32 sources at a time,
+   *    then spreads each wide one over its lanes (row-major taps; each lane
+   *    advances by 32 taps without dividing) -- no list in shared memory */
   const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
-  for (int q = warp; q < nl; q += nwarps) {
-    const uint32_t e = list[q];
-    const int kk = (int)(e >> 16), fi = (int)(e & 0xffffu);
-    const int sx = ax0 - R + kk % S, sy = ay0 - R + kk / S;
-    const float4 ki = kin[fi];
-    const int reach = (int)ki.w;
-    float4 v = load_bucket(P.buckets, P.bkind, (long long)sx + (long long)sy * P.W);
-    if (v.w == 0.0f) continue;
-    const float ls = P.k1 * log1pf(v.w * P.k2) / v.w;
-    v = make_float4(v.x * ls, v.y * ls, v.z * ls, v.w * ls);
-    const int x_lo = max(sx - reach, ax0), x_hi = min(sx + reach, ax0 + A - 1);
-    const int y_lo = max(sy - reach, ay0), y_hi = min(sy + reach, ay0 + A - 1);
-    const int wdt = x_hi - x_lo + 1;
-    const int step_y = 32 / wdt, step_x = 32 % wdt;
-    int cx = lane % wdt, y = y_lo + lane / wdt;
-    const int dx0 = x_lo - sx;
-    while (y <= y_hi) {
-      const int dx = dx0 + cx, dy = y - sy;
-      const float w = de_coef(ki, dx * dx + dy * dy);
-      if (w != 0.0f) {
-        const int o = (x_lo - ax0 + cx) + (y - ay0) * A;
-        atomicAdd(acc + o, w * v.x);
-        atomicAdd(acc + AA + o, w * v.y);
-        atomicAdd(acc + 2 * AA + o, w * v.z);
-        atomicAdd(acc + 3 * AA + o, w * v.w);
-      }
-      cx += step_x;
-      y += step_y;
-      if (cx >= wdt) {
-        cx -= wdt;
-        y++;
+  for (int base = warp * 32; base < S * S; base += nwarps * 32) {
+    DESource o;
+    bool wide = false;
+    if (base + lane < S * S && de_classify(P, cnt, kin, base + lane, S, Cc, ax0, ay0, A, R, ss, istart, iend, jstart,
+                                           jend, o))
+      wide = (o.x_hi - o.x_lo + 1) * (o.y_hi - o.y_lo + 1) > DE_SMALL_TAPS;
+    unsigned mask = __ballot_sync(0xffffffffu, wide);
+    while (mask) {
+      const int src = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const int sx = __shfl_sync(0xffffffffu, o.sx, src), sy = __shfl_sync(0xffffffffu, o.sy, src);
+      const int fi = __shfl_sync(0xffffffffu, o.fi, src);
+      const int x_lo = __shfl_sync(0xffffffffu, o.x_lo, src), x_hi = __shfl_sync(0xffffffffu, o.x_hi, src);
+      const int y_lo = __shfl_sync(0xffffffffu, o.y_lo, src), y_hi = __shfl_sync(0xffffffffu, o.y_hi, src);
+      float4 v = load_bucket(P.buckets, P.bkind, (long long)sx + (long long)sy * P.W);
+      if (v.w == 0.0f) continue;
+      const float ls = P.k1 * log1pf(v.w * P.k2) / v.w;
+      v = make_float4(v.x * ls, v.y * ls, v.z * ls, v.w * ls);
+      const float4 ki = kin[fi];
+      const int wdt = x_hi - x_lo + 1;
+      const int step_y = 32 / wdt, step_x = 32 % wdt;
+      int cx = lane % wdt, y = y_lo + lane / wdt;
+      const int dx0 = x_lo - sx;
+      while (y <= y_hi) {
+        const int dx = dx0 + cx, dy = y - sy;
+        const float w = de_coef(ki, dx * dx + dy * dy);
+        if (w != 0.0f) {
+          const int off = (x_lo - ax0 + cx) + (y - ay0) * A;
+          atomicAdd(acc + off, w * v.x);
+          atomicAdd(acc + AA + off, w * v.y);
+          atomicAdd(acc + 2 * AA + off, w * v.z);
+          atomicAdd(acc + 3 * AA + off, w * v.w);
+        }
+        cx += step_x;
+        y += step_y;
+        if (cx >= wdt) {
+          cx -= wdt;
+          y++;
+        }
       }
     }
   }
@@ -225,7 +248,8 @@ __global__ void __launch_bounds__(256) k_de_tile(DEParams P) {
 
 static size_t de_smem(int A, int R, int ss, int fw, int nk) {
   const int S = A + 2 * R, Cc = S + 2 * ss;
-  return (size_t)nk * 16 + (size_t)4 * A * A * 4 + (size_t)Cc * Cc * 4 + (size_t)fw * fw * 4 + (size_t)S * S * 4;
+  (void)S;
+  return (size_t)nk * 16 + (size_t)4 * A * A * 4 + (size_t)Cc * Cc * 4 + (size_t)fw * fw * 4;
 }
 
 static DEParams base_params(const void *buckets, int bkind, const void *count, int W, int H, int oversample,
