@@ -96,6 +96,7 @@ typedef struct {
   struct f3g_pass_info_s *h_info; size_t h_info_n;
   F3GCounters *d_ctr; F3GCounters *h_ctr;
   float *d_filter; size_t filter_bytes;
+  float *h_stage; size_t h_stage_n; /* pinned staging of small uploads (floats) */
   float *d_de_w; size_t de_w_bytes;
   float *d_de_c; size_t de_c_bytes;
   double timings[8];

@@ -5,7 +5,9 @@
  * kernels receive FP32 copies.
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include "f3g_host.h"
 
@@ -99,8 +101,81 @@ int f3g_spatial_filter(flam3_frame *spec, int field, double **filter) {
 }
 
 /* filters.c:272-407 */
+static int de_filters_build(double max_rad, double min_rad, double curve, int ss, int *max_filtered_counts,
+                            int *max_filter_index, double **widths, double **coefs);
+
+/* The filter bank depends only on (max_rad, min_rad, curve, ss) and costs up
+ * to ~2 ms to build for large radii at oversample 2: the last banks built
+ * are kept (process-wide) and handed out as copies. */
+#define DE_CACHE 32
+static struct {
+  double max_rad, min_rad, curve;
+  int ss, mfc, mfi, ks;
+  double *w, *c;
+  unsigned long long used;
+} de_cache[DE_CACHE];
+static unsigned long long de_clock;
+static pthread_mutex_t de_mu = PTHREAD_MUTEX_INITIALIZER;
+
 int f3g_de_filters(double max_rad, double min_rad, double curve, int ss, int *max_filtered_counts,
                    int *max_filter_index, double **widths, double **coefs) {
+  pthread_mutex_lock(&de_mu);
+  for (int i = 0; i < DE_CACHE; i++)
+    if (de_cache[i].w && de_cache[i].max_rad == max_rad && de_cache[i].min_rad == min_rad &&
+        de_cache[i].curve == curve && de_cache[i].ss == ss) {
+      const int n = de_cache[i].mfi + 1, ks = de_cache[i].ks;
+      double *w = (double *)malloc((size_t)n * sizeof(double));
+      double *c = (double *)malloc((size_t)n * ks * sizeof(double));
+      if (!w || !c) {
+        free(w);
+        free(c);
+        break;
+      }
+      memcpy(w, de_cache[i].w, (size_t)n * sizeof(double));
+      memcpy(c, de_cache[i].c, (size_t)n * ks * sizeof(double));
+      *widths = w;
+      *coefs = c;
+      *max_filtered_counts = de_cache[i].mfc;
+      *max_filter_index = de_cache[i].mfi;
+      de_cache[i].used = ++de_clock;
+      pthread_mutex_unlock(&de_mu);
+      return ks;
+    }
+  pthread_mutex_unlock(&de_mu);
+  const int ks = de_filters_build(max_rad, min_rad, curve, ss, max_filtered_counts, max_filter_index, widths, coefs);
+  if (ks <= 0) return ks;
+  const int n = *max_filter_index + 1;
+  double *w = (double *)malloc((size_t)n * sizeof(double));
+  double *c = (double *)malloc((size_t)n * ks * sizeof(double));
+  if (!w || !c) {
+    free(w);
+    free(c);
+    return ks;
+  }
+  memcpy(w, *widths, (size_t)n * sizeof(double));
+  memcpy(c, *coefs, (size_t)n * ks * sizeof(double));
+  pthread_mutex_lock(&de_mu);
+  int v = 0;
+  for (int i = 1; i < DE_CACHE; i++)
+    if (!de_cache[i].w || (de_cache[v].w && de_cache[i].used < de_cache[v].used)) v = i;
+  free(de_cache[v].w);
+  free(de_cache[v].c);
+  de_cache[v].max_rad = max_rad;
+  de_cache[v].min_rad = min_rad;
+  de_cache[v].curve = curve;
+  de_cache[v].ss = ss;
+  de_cache[v].mfc = *max_filtered_counts;
+  de_cache[v].mfi = *max_filter_index;
+  de_cache[v].ks = ks;
+  de_cache[v].w = w;
+  de_cache[v].c = c;
+  de_cache[v].used = ++de_clock;
+  pthread_mutex_unlock(&de_mu);
+  return ks;
+}
+
+static int de_filters_build(double max_rad, double min_rad, double curve, int ss, int *max_filtered_counts,
+                            int *max_filter_index, double **widths, double **coefs) {
   const int keep = 100;
   if (curve <= 0.0) {
     f3g_set_error("estimator curve must be > 0");

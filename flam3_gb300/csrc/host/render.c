@@ -349,16 +349,27 @@ int f3g_build_batch_passes(flam3_frame *spec, int field, const f3g_geom *g, int 
   return 0;
 }
 
-static float *upload_floats(f3g_ctx *c, float **dptr, size_t *cap, const double *src, size_t n) {
-  float *tmp = (float *)malloc(n * sizeof(float));
-  for (size_t i = 0; i < n; i++) tmp[i] = (float)src[i];
-  if (f3g_ensure((void **)dptr, cap, n * sizeof(float))) {
-    free(tmp);
-    return NULL;
+/* Copies n values as floats to a device buffer through the context's pinned
+ * staging area at float offset `slot` (so the copy is truly asynchronous);
+ * a slot may be reused only after the stream has passed the copy. */
+static float *upload_floats(f3g_ctx *c, float **dptr, size_t *cap, const double *src, size_t n, size_t slot) {
+  if (slot + n > c->h_stage_n) {
+    size_t want = slot + n < 4096 ? 4096 : 2 * (slot + n);
+    float *nb = NULL;
+    cudaStreamSynchronize(c->stream); /* the old staging area may still be read */
+    if (cudaMallocHost((void **)&nb, want * sizeof(float)) != cudaSuccess) {
+      f3g_set_error("cudaMallocHost of %zu floats failed", want);
+      return NULL;
+    }
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nb;
+    c->h_stage_n = want;
   }
+  float *tmp = c->h_stage + slot;
+  for (size_t i = 0; i < n; i++) tmp[i] = (float)src[i];
+  if (f3g_ensure((void **)dptr, cap, n * sizeof(float))) return NULL;
   cudaError_t e = cudaMemcpyAsync(*dptr, tmp, n * sizeof(float), cudaMemcpyHostToDevice, c->stream);
-  cudaStreamSynchronize(c->stream);
-  free(tmp);
+  if (e != cudaSuccess) f3g_set_error("filter upload failed: %s", cudaGetErrorString(e));
   return e == cudaSuccess ? *dptr : NULL;
 }
 
@@ -457,15 +468,21 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
   if (f3g_ensure(&c->d_acc, &c->acc_bytes, (size_t)nb * bsz)) goto done;
   size_t out_bytes = (size_t)g.image_width * g.image_height * nchan * spec->bytes_per_channel;
   if (f3g_ensure((void **)&c->d_out, &c->out_bytes, out_bytes)) goto done;
-  if (!upload_floats(c, &c->d_filter, &c->filter_bytes, filter, (size_t)g.filter_width * g.filter_width)) goto done;
+  const size_t filter_n = (size_t)g.filter_width * g.filter_width;
+  const size_t kinfo_slot = (filter_n + 63) & ~(size_t)63;
+  if (!upload_floats(c, &c->d_filter, &c->filter_bytes, filter, filter_n, 0)) goto done;
   h2d += (double)g.filter_width * g.filter_width * sizeof(float);
-  CK(cudaMemsetAsync(c->d_acc, 0, (size_t)nb * bsz, c->stream));
+  int acc_cleared = 0; /* the accumulator is cleared only when a path uses it */
   if (ensure_host_passes(c, (size_t)ntemporal)) goto done;
   if (f3g_ensure((void **)&c->d_passes, &c->passes_bytes, (size_t)ntemporal * sizeof(F3GPass))) goto done;
   if (f3g_ensure((void **)&c->d_prefix, &c->prefix_bytes, (size_t)(ntemporal + 1) * sizeof(long long))) goto done;
   if (f3g_ensure((void **)&c->d_items, &c->d_items_bytes, (size_t)ntemporal * sizeof(F3GItem))) goto done;
   const int precision = f3g_opts.iter_precision == 64 ? 64 : 32;
   const int de_tile = f3g_opts.de_tile > 0 ? f3g_opts.de_tile : 16;
+  /* a one-batch render without a progress callback runs uploads, iterate,
+   * tail and copy-out back to back and waits once */
+  const int deferred_iter = nbatches == 1 && !spec->progress && !(io && (io->hist_out || io->accum_out));
+  int pending_ctr = 0;
   double vibrancy = 0.0, gamma = 0.0, background[3] = {0, 0, 0};
   int vib_gam_n = 0;
   double ppux = 0, ppuy = 0, sample_density = 0;
@@ -599,6 +616,12 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         }
         CK(cudaEventRecord(c->ev[1], c->stream));
         CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr, sizeof(F3GCounters), cudaMemcpyDeviceToHost, c->stream));
+        if (deferred_iter) {
+          /* one batch, no progress callback: the tail is queued right behind
+           * this launch; the counters are read after the final wait */
+          pending_ctr = 1;
+          continue;
+        }
         CK(cudaStreamSynchronize(c->stream));
         float ms = 0;
         cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
@@ -679,7 +702,9 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         double *kid = (double *)malloc((size_t)nk * 4 * sizeof(double));
         f3g_de_kernel_info(mfi, ks, de_w, de_c, ki);
         for (int i = 0; i < 4 * nk; i++) kid[i] = ki[i];
-        float *ok = upload_floats(c, &c->d_de_w, &c->de_w_bytes, kid, (size_t)nk * 4);
+        /* several batches reuse the slot: wait for the previous batch's copy */
+        if (batch > 0) cudaStreamSynchronize(c->stream);
+        float *ok = upload_floats(c, &c->d_de_w, &c->de_w_bytes, kid, (size_t)nk * 4, kinfo_slot);
         free(ki);
         free(kid);
         if (!ok) goto done;
@@ -697,6 +722,10 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         fde_count = use_count;
         goto tail_fused;
       }
+    }
+    if (!acc_cleared) {
+      CK(cudaMemsetAsync(c->d_acc, 0, (size_t)nb * bsz, c->stream));
+      acc_cleared = 1;
     }
     CK(cudaEventRecord(c->ev[2], c->stream));
     if (de_on) {
@@ -800,6 +829,13 @@ tail_fused:;
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]);
     t_tail = ms;
+    if (pending_ctr) {
+      float mi = 0;
+      cudaEventElapsedTime(&mi, c->ev[0], c->ev[1]);
+      t_iter += mi;
+      stats->badvals += (double)c->h_ctr->badvals;
+      plotted += (double)c->h_ctr->plotted;
+    }
   }
   rv = 0;
 
