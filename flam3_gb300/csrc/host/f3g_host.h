@@ -97,6 +97,7 @@ typedef struct {
   F3GCounters *d_ctr; F3GCounters *h_ctr;
   float *d_filter; size_t filter_bytes;
   float *h_stage; size_t h_stage_n; /* pinned staging of small uploads (floats) */
+  unsigned char *h_img; size_t h_img_bytes; /* pinned staging of the image */
   float *d_de_w; size_t de_w_bytes;
   float *d_de_c; size_t de_c_bytes;
   double timings[8];

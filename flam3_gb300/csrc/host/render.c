@@ -822,10 +822,27 @@ tail_fused:;
     unsigned char *dst = (unsigned char *)out;
     if (field == flam3_field_odd) dst += row;
     size_t dpitch = (size_t)g.out_width * nchan * spec->bytes_per_channel;
-    CK(cudaMemcpy2DAsync(dst, dpitch, c->d_out, row, row, (size_t)g.image_height, cudaMemcpyDeviceToHost,
-                               c->stream));
-    d2h += (double)row * g.image_height;
-    CK(cudaStreamSynchronize(c->stream));
+    const size_t img_bytes = row * (size_t)g.image_height;
+    /* through pinned staging: a DMA at full speed, then one host copy (a
+     * direct copy into pageable memory runs at a fraction of the link) */
+    if (img_bytes > c->h_img_bytes) {
+      if (c->h_img) cudaFreeHost(c->h_img);
+      c->h_img = NULL;
+      c->h_img_bytes = 0;
+      if (cudaMallocHost((void **)&c->h_img, img_bytes) == cudaSuccess) c->h_img_bytes = img_bytes;
+    }
+    if (c->h_img) {
+      CK(cudaMemcpyAsync(c->h_img, c->d_out, img_bytes, cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      if (dpitch == row) memcpy(dst, c->h_img, img_bytes);
+      else
+        for (int y = 0; y < g.image_height; y++) memcpy(dst + (size_t)y * dpitch, c->h_img + (size_t)y * row, row);
+    } else {
+      CK(cudaMemcpy2DAsync(dst, dpitch, c->d_out, row, row, (size_t)g.image_height, cudaMemcpyDeviceToHost,
+                           c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    }
+    d2h += (double)img_bytes;
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]);
     t_tail = ms;

@@ -724,6 +724,16 @@ static int admit_job(flam3gpu_service *s, f3g_job *j) {
   } else
     ok = 0;
   s->c_h2d += (double)npass * pass_bytes + (double)j->g.filter_width * j->g.filter_width * 4 + j->nkinfo * 4.0;
+  if (ok) {
+    /* copies from pageable memory return once the data is staged: the host
+     * tables are no longer needed */
+    free(j->h_passes);
+    free(j->h_filter);
+    free(j->h_kinfo);
+    j->h_passes = NULL;
+    j->h_filter = NULL;
+    j->h_kinfo = NULL;
+  }
   if (!ok) {
     snprintf(j->err, sizeof(j->err), "device setup failed: %s", cudaGetErrorString(cudaGetLastError()));
     return 1;
