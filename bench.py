@@ -244,6 +244,23 @@ def run_gpu(args):
     tail_gbs = args.steps * (hist_bytes + out_bytes) / tail_s / 1e9 if tail_s > 0 else None
     value = iters / dev_s / 1e9
     e2e = iters / wall_s / 1e9
+    # the same genome and size without density estimation: the fused
+    # log-scale + filter + tonemap + pack kernel, an HBM-streaming pass
+    nodde = None
+    if world == 1:
+        Gn = gm.config1_genome(1, estimator=0.0)
+        tails = []
+        for s_ in range(args.warmup + args.steps):
+            flush_l2(flush)
+            render.render(gm.Frame(Gn, bits=33, seed="nodde-%d" % s_))
+            tails.append(render.last_timings()["tail_ms"])
+        t_nd = statistics.median(tails[args.warmup:]) / 1e3
+        nd_bytes = hist_bytes + out_bytes
+        nodde = {"bound": "hbm", "kernel": "k_fused_log_filter (log scale + filter + tonemap + pack, no DE)",
+                 "achieved": nd_bytes / t_nd / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                 "frac": nd_bytes / t_nd / 1e9 / hbm_peak, "traffic": None, "ms": t_nd * 1e3,
+                 "note": f"config-1 genome and size with estimator 0: histogram {hist_bytes / 1e6:.1f} MB read + "
+                         f"image {out_bytes / 1e6:.1f} MB write; peak {peak_kind}; L2 flushed before each render"}
     cb = None
     if world == 1 and not args.no_cpu:
         cb, _ = cpu_baseline(steps=1)
@@ -264,6 +281,7 @@ def run_gpu(args):
                           "frac": (tail_gbs / hbm_peak) if tail_gbs else None, "traffic": TAIL_TRAFFIC,
                           "note": f"histogram {hist_bytes / 1e6:.1f} MB read + image {out_bytes / 1e6:.1f} MB "
                                   f"write per render; peak {peak_kind}"},
+        "roofline_tail_no_de": nodde,
         "e2e": {"value": e2e, "unit": "Giter/s", "h2d_bytes_per_step": int(recs[0][2]["h2d_bytes"]),
                 "d2h_bytes_per_step": int(recs[0][2]["d2h_bytes"])},
         "gpu_launches": int(sum(r[2]["launches"] for r in recs)),
