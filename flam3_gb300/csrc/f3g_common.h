@@ -127,6 +127,11 @@ typedef struct {
 /* bytes of a pass that hold data when its genome has nx xforms */
 #define F3G_PASS_BYTES(nx) (offsetof(F3GPass, xf) + (size_t)(nx) * sizeof(F3GXform))
 
+/* The spatial filter as uploaded: the fw x fw filter (index i + j*fw, i
+ * horizontal) followed by its vertical factor fu[fw] and horizontal factor
+ * fv[fw], with filter[i + j*fw] == fu[j] * fv[i]. */
+#define F3G_FILTER_FLOATS(fw) ((size_t)(fw) * (size_t)(fw) + 2 * (size_t)(fw))
+
 /* One entry of an iterate launch's work list: chunks [chunk_first,
  * chunk_first + n) of a pass, where n is the entry's span in the launch's
  * chunk prefix.  Chunk k of a pass always draws the same random stream, so a

@@ -56,6 +56,19 @@ int f3g_launch_de_fused_tile(const void *buckets, int bkind, const void *count, 
 /* raises the tail kernels' shared-memory limits (call before stream capture) */
 int f3g_de_prepare(void);
 int f3g_tail_prepare(void);
+/* separable strip kernels (f3g_strip_{f32,f64}{,e}.cu: FP32/FP64
+ * histogram, earlyclip off/on): -2 when no instantiation covers
+ * (oversample, fw) */
+#define F3G_STRIP_DECL(SUFFIX)                                                                                  \
+  int f3g_strip_prepare_##SUFFIX(void);                                                                       \
+  int f3g_strip_launch_##SUFFIX(const void *buckets, int W, int H, double k1, double k2, int de_offset,       \
+                                int oversample, const float *filter, int fw, int image_w, int image_h,        \
+                                unsigned char *out, const F3GTonemap *tp, cudaStream_t st);
+F3G_STRIP_DECL(f32)
+F3G_STRIP_DECL(f64)
+F3G_STRIP_DECL(f32e)
+F3G_STRIP_DECL(f64e)
+#undef F3G_STRIP_DECL
 int f3g_launch_earlyclip(void *acc, int akind, long long n, const F3GTonemap *tp, cudaStream_t st);
 int f3g_launch_filter_tonemap(const void *acc, int akind, int W, int de_offset, int oversample, const float *filter,
                               int fw, int image_w, int image_h, unsigned char *out, int earlyclip,

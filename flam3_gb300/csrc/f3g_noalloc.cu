@@ -169,7 +169,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
       cv.take((size_t)(ntemporal + 1) * sizeof(long long));
       cv.take((size_t)ntemporal * sizeof(F3GItem));
       cv.take(sizeof(F3GCounters));
-      cv.take((size_t)g.filter_width * g.filter_width * sizeof(float));
+      cv.take(F3G_FILTER_FLOATS(g.filter_width) * sizeof(float));
       cv.take(de_on ? (size_t)(mfi + 1) * 4 * sizeof(float) : 0);
       cv.take((size_t)nb * bsz);
       cv.take(de_on ? (size_t)nb * csz : 0);
@@ -186,7 +186,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     long long *d_prefix = (long long *)cv.take((size_t)(ntemporal + 1) * sizeof(long long));
     F3GItem *d_items = (F3GItem *)cv.take((size_t)ntemporal * sizeof(F3GItem));
     F3GCounters *d_ctr = (F3GCounters *)cv.take(sizeof(F3GCounters));
-    float *d_filter = (float *)cv.take((size_t)g.filter_width * g.filter_width * sizeof(float));
+    float *d_filter = (float *)cv.take(F3G_FILTER_FLOATS(g.filter_width) * sizeof(float));
     float *d_de = (float *)cv.take(de_on ? (size_t)(mfi + 1) * 4 * sizeof(float) : 0);
     void *d_hist = cv.take((size_t)nb * bsz);
     void *d_count = cv.take(de_on ? (size_t)nb * csz : 0);
@@ -196,7 +196,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     passes = (F3GPass *)malloc((size_t)ntemporal * sizeof(F3GPass));
     prefix = (long long *)malloc((size_t)(ntemporal + 1) * sizeof(long long));
     items = (F3GItem *)malloc((size_t)ntemporal * sizeof(F3GItem));
-    const size_t nf = (size_t)g.filter_width * g.filter_width + (de_on ? (size_t)(mfi + 1) * 4 : 0);
+    const size_t nf = F3G_FILTER_FLOATS(g.filter_width) + (de_on ? (size_t)(mfi + 1) * 4 : 0);
     fbuf = (float *)malloc(nf * sizeof(float));
     if (!passes || !prefix || !items || !fbuf) {
       f3g_set_error("host memory exhausted");
@@ -258,9 +258,9 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
       total_chunks += passes[ts].nchunks;
     }
     prefix[ntemporal] = total_chunks;
-    for (size_t i = 0; i < (size_t)g.filter_width * g.filter_width; i++) fbuf[i] = (float)filter[i];
+    for (size_t i = 0; i < F3G_FILTER_FLOATS(g.filter_width); i++) fbuf[i] = (float)filter[i];
     if (de_on) {
-      f3g_de_kernel_info(mfi, ks, de_w, de_c, fbuf + (size_t)g.filter_width * g.filter_width);
+      f3g_de_kernel_info(mfi, ks, de_w, de_c, fbuf + F3G_FILTER_FLOATS(g.filter_width));
     }
     F3GCounters ctr;
     memset(&ctr, 0, sizeof(ctr));
@@ -271,9 +271,9 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     NCK(cudaMemcpy(d_prefix, prefix, (size_t)(ntemporal + 1) * sizeof(long long), cudaMemcpyHostToDevice));
     NCK(cudaMemcpy(d_items, items, (size_t)ntemporal * sizeof(F3GItem), cudaMemcpyHostToDevice));
     NCK(cudaMemcpy(d_ctr, &ctr, sizeof(ctr), cudaMemcpyHostToDevice));
-    NCK(cudaMemcpy(d_filter, fbuf, (size_t)g.filter_width * g.filter_width * sizeof(float), cudaMemcpyHostToDevice));
+    NCK(cudaMemcpy(d_filter, fbuf, F3G_FILTER_FLOATS(g.filter_width) * sizeof(float), cudaMemcpyHostToDevice));
     if (de_on)
-      NCK(cudaMemcpy(d_de, fbuf + (size_t)g.filter_width * g.filter_width,
+      NCK(cudaMemcpy(d_de, fbuf + F3G_FILTER_FLOATS(g.filter_width),
                      (size_t)(mfi + 1) * 4 * sizeof(float), cudaMemcpyHostToDevice));
     const int shuffle = f3g_opts.shuffle_every > 0 ? f3g_opts.shuffle_every : 1;
     int e = f3g_launch_iterate(d_items, d_prefix, ntemporal, total_chunks, shuffle, precision, full, mode, threads,

@@ -1,0 +1,12 @@
+/*
+ * f3g_strip_f32e.cu -- separable strip kernels for FP32 histograms, earlyclip.
+ */
+#include "f3g_strip.cuh"
+
+#define F3G_STRIP_OCC(SSV, FWV) strip_occupancy<SSV, FWV, false, true>();
+#define F3G_STRIP_CASE(SSV, FWV)                                                                              \
+  if (oversample == SSV && fw == FWV)                                                                         \
+    return launch_strip<SSV, FWV, false, true>(buckets, W, H, k1, k2, de_offset, filter, image_w, image_h, out, tp, \
+                                        st);
+
+F3G_STRIP_ENTRIES(f32e, false, true)

@@ -13,6 +13,10 @@
  *   k_filter_tonemap  spatial filter + tonemap + pack      (one output pixel per thread)
  *   k_fused_log_filter: log scaling + filter + tonemap + pack in one pass over
  *                     the histogram, for one batch without DE
+ *   k_log_filter_strip (f3g_strip.cuh): the same pass with the filter
+ *                     applied as its two 1-D factors, streaming histogram
+ *                     rows through shared memory; used for oversample 1
+ *                     with filter widths 1..7 and oversample 2 with 2..16
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -123,6 +127,7 @@ __global__ void __launch_bounds__(256) k_fused_log_filter(const void *__restrict
   pack_pixel(out + (size_t)tp.nchan * tp.bpc * ((size_t)i + (size_t)j * image_w), t, tp);
 }
 
+
 }  // namespace f3g
 
 using namespace f3g;
@@ -162,6 +167,8 @@ extern "C" int f3g_tail_prepare(void) {
   if (fused_log_attr_done) return 0;
   cudaError_t e = cudaFuncSetAttribute(k_fused_log_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (e != cudaSuccess) return (int)e;
+  if (f3g_strip_prepare_f32() || f3g_strip_prepare_f64() || f3g_strip_prepare_f32e() || f3g_strip_prepare_f64e())
+    return (int)cudaErrorUnknown;
   fused_log_attr_done = 1;
   return 0;
 }
@@ -170,11 +177,16 @@ extern "C" int f3g_launch_fused_log_filter(const void *buckets, int bkind, int W
                                            int de_offset, int oversample, const float *filter, int fw, int image_w,
                                            int image_h, unsigned char *out, int earlyclip, const F3GTonemap *tp,
                                            cudaStream_t st) {
+  int e = f3g_tail_prepare();
+  if (e) return e;
+  /* the separable strip kernel where an instantiation exists */
+  e = (bkind == F3G_BK_F32 ? (earlyclip ? f3g_strip_launch_f32e : f3g_strip_launch_f32)
+                            : (earlyclip ? f3g_strip_launch_f64e : f3g_strip_launch_f64))(
+      buckets, W, H, k1, k2, de_offset, oversample, filter, fw, image_w, image_h, out, tp, st);
+  if (e != -2) return e;
   int sw = FL_TX * oversample + fw - oversample, sh = FL_TY * oversample + fw - oversample;
   size_t smem = (size_t)sw * sh * sizeof(float4) + (size_t)fw * fw * sizeof(float);
   if (smem > 200 * 1024) return -1;
-  int e = f3g_tail_prepare();
-  if (e) return e;
   dim3 block(FL_TX, FL_TY), grid((image_w + FL_TX - 1) / FL_TX, (image_h + FL_TY - 1) / FL_TY);
   k_fused_log_filter<<<grid, block, smem, st>>>(buckets, bkind, W, H, (float)k1, (float)k2, de_offset, oversample,
                                                 filter, fw, image_w, image_h, out, earlyclip, *tp);

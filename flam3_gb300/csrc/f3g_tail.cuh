@@ -54,9 +54,41 @@ __device__ __forceinline__ void acc_store(void *acc, int kind, long long i, floa
   }
 }
 
+/* Tail arithmetic is FP32 with hardware approximations (a few ulp) unless
+ * F3G_ACCURATE_MATH is defined; the output is quantised to 8 or 16 bits. */
+#ifndef F3G_ACCURATE_MATH
+__device__ __forceinline__ float t_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float t_pow(float x, float y) { return __powf(x, y); }
+/* log(1 + x) for x >= 0: below 1 from log1p(x) = 2 atanh(s), s = x / (2 + x)
+ * <= 1/3, with the atanh Taylor series to s^13 (truncation < 2e-8
+ * relative); above 1 from the hardware logarithm, whose relative error is
+ * small there because the result exceeds ln 2. */
+__device__ __forceinline__ float t_log1p(float x) {
+  if (x >= 1.0f) return __logf(1.0f + x);
+  const float s = __fdividef(x, 2.0f + x), z = s * s;
+  float p = 1.0f / 13.0f;
+  p = fmaf(p, z, 1.0f / 11.0f);
+  p = fmaf(p, z, 1.0f / 9.0f);
+  p = fmaf(p, z, 1.0f / 7.0f);
+  p = fmaf(p, z, 1.0f / 5.0f);
+  p = fmaf(p, z, 1.0f / 3.0f);
+  p = fmaf(p, z, 1.0f);
+  return 2.0f * s * p;
+}
+#else
+__device__ __forceinline__ float t_div(float a, float b) { return a / b; }
+__device__ __forceinline__ float t_pow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ float t_log1p(float x) { return log1pf(x); }
+#endif
+
 /* ls = k1 * log(1 + c3*k2) / c3  (rect.c:963) */
 __device__ __forceinline__ float log_scale(float c3, float k1, float k2) {
-  return k1 * log1pf(c3 * k2) / c3;
+  return t_div(k1 * t_log1p(c3 * k2), c3);
+}
+
+/* log_scale for any c3 >= 0, 0 for an empty bucket */
+__device__ __forceinline__ float log_scale_nz(float c3, float k1, float k2) {
+  return c3 != 0.0f ? log_scale(c3, k1, k2) : 0.0f;
 }
 
 /* ---------------------------------------------------------------------
@@ -70,10 +102,11 @@ __device__ __forceinline__ void rgb2hsv(const float *rgb, float *hsv) {
   else mn = (gd <= bd) ? gd : bd;
   del = mx - mn;
   v = mx;
-  s = (mx != 0.0f) ? del / mx : 0.0f;
+  s = (mx != 0.0f) ? t_div(del, mx) : 0.0f;
   h = 0.0f;
   if (s != 0.0f) {
-    float rc = (mx - rd) / del, gc = (mx - gd) / del, bc = (mx - bd) / del;
+    const float id = t_div(1.0f, del);
+    float rc = (mx - rd) * id, gc = (mx - gd) * id, bc = (mx - bd) * id;
     if (rd == mx) h = bc - gc;
     else if (gd == mx) h = 2.0f + rc - bc;
     else if (bd == mx) h = 4.0f + gc - rc;
@@ -104,10 +137,10 @@ __device__ __forceinline__ void hsv2rgb(const float *hsv, float *rgb) {
 __device__ __forceinline__ float calc_alpha(float density, float gamma, float linrange, float funcval) {
   if (density > 0.0f) {
     if (density < linrange) {
-      float frac = density / linrange;
-      return (1.0f - frac) * density * (funcval / linrange) + frac * powf(density, gamma);
+      float frac = t_div(density, linrange);
+      return (1.0f - frac) * density * t_div(funcval, linrange) + frac * t_pow(density, gamma);
     }
-    return powf(density, gamma);
+    return t_pow(density, gamma);
   }
   return 0.0f;
 }
@@ -119,40 +152,40 @@ __device__ __forceinline__ void calc_newrgb(const float *cbuf, float ls, float h
   }
   float maxa = -1.0f, maxc = 0.0f;
   for (int k = 0; k < 3; k++) {
-    float a = ls * (cbuf[k] / 255.0f);
-    if (a > maxa) { maxa = a; maxc = cbuf[k] / 255.0f; }
+    float a = ls * (cbuf[k] * (1.0f / 255.0f));
+    if (a > maxa) { maxa = a; maxc = cbuf[k] * (1.0f / 255.0f); }
   }
   if (maxa > 255.0f && highpow >= 0.0f) {
-    float newls = 255.0f / maxc, lsratio = powf(newls / ls, highpow), hsv[3];
-    for (int k = 0; k < 3; k++) newrgb[k] = newls * (cbuf[k] / 255.0f) / 255.0f;
+    float newls = t_div(255.0f, maxc), lsratio = t_pow(t_div(newls, ls), highpow), hsv[3];
+    for (int k = 0; k < 3; k++) newrgb[k] = newls * (cbuf[k] * (1.0f / 255.0f)) * (1.0f / 255.0f);
     rgb2hsv(newrgb, hsv);
     hsv[1] *= lsratio;
     hsv2rgb(hsv, newrgb);
     for (int k = 0; k < 3; k++) newrgb[k] *= 255.0f;
   } else {
-    float newls = 255.0f / maxc, adjhlp = -highpow;
+    float newls = t_div(255.0f, maxc), adjhlp = -highpow;
     if (adjhlp > 1.0f) adjhlp = 1.0f;
     if (maxa <= 255.0f) adjhlp = 1.0f;
-    for (int k = 0; k < 3; k++) newrgb[k] = ((1.0f - adjhlp) * newls + adjhlp * ls) * (cbuf[k] / 255.0f);
+    for (int k = 0; k < 3; k++) newrgb[k] = ((1.0f - adjhlp) * newls + adjhlp * ls) * (cbuf[k] * (1.0f / 255.0f));
   }
 }
 
 __device__ __forceinline__ void tonemap(float *t, const F3GTonemap &tp) {
-  float alpha, ls, tmp = t[3] / 255.0f, newrgb[3];
+  float alpha, ls, tmp = t[3] * (1.0f / 255.0f), newrgb[3];
   if (t[3] <= 0.0f) {
     alpha = 0.0f;
     ls = 0.0f;
   } else {
     alpha = calc_alpha(tmp, tp.g, tp.linrange, tp.funcval);
-    ls = tp.vibrancy * 256.0f * alpha / tmp;
+    ls = t_div(tp.vibrancy * 256.0f * alpha, tmp);
     alpha = fminf(fmaxf(alpha, 0.0f), 1.0f);
   }
   calc_newrgb(t, ls, tp.highpow, newrgb);
   for (int k = 0; k < 3; k++) {
     float a = newrgb[k];
-    if (tp.vibrancy != 1.0f) a += (1.0f - tp.vibrancy) * 256.0f * powf(t[k] / 255.0f, tp.g);
+    if (tp.vibrancy != 1.0f) a += (1.0f - tp.vibrancy) * 256.0f * t_pow(t[k] * (1.0f / 255.0f), tp.g);
     if (tp.nchan <= 3 || tp.transp == 0) a += (1.0f - alpha) * tp.background[k];
-    else a = (alpha > 0.0f) ? a / alpha : 0.0f;
+    else a = (alpha > 0.0f) ? t_div(a, alpha) : 0.0f;
     t[k] = fminf(fmaxf(a, 0.0f), 255.0f);
   }
   t[3] = alpha;

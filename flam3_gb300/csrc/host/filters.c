@@ -78,24 +78,38 @@ int f3g_spatial_filter(flam3_frame *spec, int field, double **filter) {
   int fwidth = ((int)fw) + 1;
   if ((fwidth ^ ss) & 1) fwidth++;
   adjust = fw > 0.0 ? supp * fwidth / fw : 1.0;
-  double *f = (double *)calloc((size_t)fwidth * fwidth, sizeof(double));
-  double sum = 0.0;
+  /* fw x fw filter, then its vertical and horizontal factors */
+  double *f = (double *)calloc(F3G_FILTER_FLOATS(fwidth), sizeof(double));
+  if (!f) {
+    f3g_set_error("out of host memory");
+    return -1;
+  }
+  double *fu = f + (size_t)fwidth * fwidth, *fv = fu + fwidth;
+  double sum = 0.0, sum_h = 0.0;
+  for (int i = 0; i < fwidth; i++) {
+    double ii = ((2.0 * i + 1.0) / (double)fwidth - 1.0) * adjust;
+    double jj = ((2.0 * i + 1.0) / (double)fwidth - 1.0) * adjust;
+    if (field) jj *= 2.0;
+    jj /= aspect;
+    fv[i] = kernel(knum, ii);
+    fu[i] = kernel(knum, jj);
+    sum_h += fv[i];
+  }
   for (int i = 0; i < fwidth; i++)
-    for (int j = 0; j < fwidth; j++) {
-      double ii = ((2.0 * i + 1.0) / (double)fwidth - 1.0) * adjust;
-      double jj = ((2.0 * j + 1.0) / (double)fwidth - 1.0) * adjust;
-      if (field) jj *= 2.0;
-      jj /= aspect;
-      f[i + j * fwidth] = kernel(knum, ii) * kernel(knum, jj);
-    }
+    for (int j = 0; j < fwidth; j++) f[i + j * fwidth] = fv[i] * fu[j];
   for (int i = 0; i < fwidth * fwidth; i++) sum += f[i];
-  if (sum == 0.0) {
+  if (sum == 0.0 || sum_h == 0.0) {
     free(f);
     f3g_set_error("Spatial filter value is too small: %g.", radius);
     return -1;
   }
   sum = 1.0 / sum;
   for (int i = 0; i < fwidth * fwidth; i++) f[i] *= sum;
+  /* fu[j] * fv[i] == f[i + j*fw]: the horizontal factor sums to one */
+  for (int i = 0; i < fwidth; i++) {
+    fu[i] *= sum * sum_h;
+    fv[i] /= sum_h;
+  }
   *filter = f;
   return fwidth;
 }

@@ -468,10 +468,10 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
   if (f3g_ensure(&c->d_acc, &c->acc_bytes, (size_t)nb * bsz)) goto done;
   size_t out_bytes = (size_t)g.image_width * g.image_height * nchan * spec->bytes_per_channel;
   if (f3g_ensure((void **)&c->d_out, &c->out_bytes, out_bytes)) goto done;
-  const size_t filter_n = (size_t)g.filter_width * g.filter_width;
+  const size_t filter_n = F3G_FILTER_FLOATS(g.filter_width);
   const size_t kinfo_slot = (filter_n + 63) & ~(size_t)63;
   if (!upload_floats(c, &c->d_filter, &c->filter_bytes, filter, filter_n, 0)) goto done;
-  h2d += (double)g.filter_width * g.filter_width * sizeof(float);
+  h2d += (double)filter_n * sizeof(float);
   int acc_cleared = 0; /* the accumulator is cleared only when a path uses it */
   if (ensure_host_passes(c, (size_t)ntemporal)) goto done;
   if (f3g_ensure((void **)&c->d_passes, &c->passes_bytes, (size_t)ntemporal * sizeof(F3GPass))) goto done;

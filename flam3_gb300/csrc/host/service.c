@@ -339,13 +339,13 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
   j->h_passes = (F3GPass *)calloc((size_t)npass, sizeof(F3GPass));
   j->pass_prefix = (long long *)calloc((size_t)nbatches * (ntemporal + 1), sizeof(long long));
   j->bp = (batch_plan *)calloc((size_t)nbatches, sizeof(batch_plan));
-  j->h_filter = (float *)malloc((size_t)g.filter_width * g.filter_width * sizeof(float));
+  j->h_filter = (float *)malloc(F3G_FILTER_FLOATS(g.filter_width) * sizeof(float));
   info = (f3g_pass_info *)calloc((size_t)ntemporal, sizeof(f3g_pass_info));
   if (!j->h_passes || !j->pass_prefix || !j->bp || !j->h_filter || !info) {
     f3g_set_error("host memory exhausted");
     goto done;
   }
-  for (int i = 0; i < g.filter_width * g.filter_width; i++) j->h_filter[i] = (float)filter[i];
+  for (size_t i = 0; i < F3G_FILTER_FLOATS(g.filter_width); i++) j->h_filter[i] = (float)filter[i];
   double vibrancy = 0.0, gamma = 0.0, background[3] = {0, 0, 0};
   int vib_gam_n = 0;
   double ppux = 0, ppuy = 0, sample_density = 0;
@@ -507,7 +507,7 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
   j->dev_bytes = align256((size_t)npass * sizeof(F3GPass)) + align256((size_t)j->nb * j->bsz) +
                  (j->count_any ? align256((size_t)j->nb * j->csz) : 0) +
                  (j->need_acc ? align256((size_t)j->nb * j->bsz) : 0) + align256(j->out_bytes) +
-                 align256((size_t)g.filter_width * g.filter_width * sizeof(float)) +
+                 align256(F3G_FILTER_FLOATS(g.filter_width) * sizeof(float)) +
                  align256(j->nkinfo * sizeof(float)) + 256;
   rv = 0;
 done:
@@ -684,7 +684,7 @@ static int admit_job(flam3gpu_service *s, f3g_job *j) {
   if (j->count_any) CARVE(j->d_count, void *, (size_t)j->nb * j->csz);
   if (j->need_acc) CARVE(j->d_acc, void *, (size_t)j->nb * j->bsz);
   CARVE(j->d_out, unsigned char *, j->out_bytes);
-  CARVE(j->d_filter, float *, (size_t)j->g.filter_width * j->g.filter_width * sizeof(float));
+  CARVE(j->d_filter, float *, F3G_FILTER_FLOATS(j->g.filter_width) * sizeof(float));
   CARVE(j->d_kinfo, float *, j->nkinfo * sizeof(float));
   CARVE(j->d_counts, unsigned long long *, 2 * sizeof(unsigned long long));
 #undef CARVE
@@ -701,7 +701,7 @@ static int admit_job(flam3gpu_service *s, f3g_job *j) {
   const size_t pass_bytes = F3G_PASS_BYTES(nxmax);
   int ok = cudaMemcpy2DAsync(j->d_passes, sizeof(F3GPass), j->h_passes, sizeof(F3GPass), pass_bytes, (size_t)npass,
                              cudaMemcpyHostToDevice, s->s_up) == cudaSuccess;
-  ok = ok && cudaMemcpyAsync(j->d_filter, j->h_filter, (size_t)j->g.filter_width * j->g.filter_width * sizeof(float),
+  ok = ok && cudaMemcpyAsync(j->d_filter, j->h_filter, F3G_FILTER_FLOATS(j->g.filter_width) * sizeof(float),
                              cudaMemcpyHostToDevice, s->s_up) == cudaSuccess;
   if (j->nkinfo)
     ok = ok && cudaMemcpyAsync(j->d_kinfo, j->h_kinfo, j->nkinfo * sizeof(float), cudaMemcpyHostToDevice,
@@ -723,7 +723,7 @@ static int admit_job(flam3gpu_service *s, f3g_job *j) {
     cudaEventDestroy(ev);
   } else
     ok = 0;
-  s->c_h2d += (double)npass * pass_bytes + (double)j->g.filter_width * j->g.filter_width * 4 + j->nkinfo * 4.0;
+  s->c_h2d += (double)npass * pass_bytes + (double)F3G_FILTER_FLOATS(j->g.filter_width) * 4 + j->nkinfo * 4.0;
   if (ok) {
     /* copies from pageable memory return once the data is staged: the host
      * tables are no longer needed */
