@@ -256,7 +256,7 @@ def run_gpu(args):
             tails.append(render.last_timings()["tail_ms"])
         t_nd = statistics.median(tails[args.warmup:]) / 1e3
         nd_bytes = hist_bytes + out_bytes
-        nodde = {"bound": "hbm", "kernel": "k_fused_log_filter (log scale + filter + tonemap + pack, no DE)",
+        nodde = {"bound": "hbm", "kernel": "k_log_filter_strip (log scale + separable filter + tonemap + pack, no DE)",
                  "achieved": nd_bytes / t_nd / 1e9, "peak": hbm_peak, "unit": "GB/s",
                  "frac": nd_bytes / t_nd / 1e9 / hbm_peak, "traffic": None, "ms": t_nd * 1e3,
                  "note": f"config-1 genome and size with estimator 0: histogram {hist_bytes / 1e6:.1f} MB read + "
