@@ -323,3 +323,260 @@ int flam3gpu_colorhist(flam3_genome *cp, int num_batches, randctx *rc, double *h
   return 0;
 }
 
+/* flam3_dimension (flam3.h:592, flam3.c:3949-4052): the correlation
+ * dimension from ntries attractor points (chains of 10000 samples after 20
+ * fuse steps, optionally clipped to the camera) and ntries random pairs:
+ * 0.434294 * log(n2 / (n1 - 0.5)), n2 / n1 counting pairs closer than
+ * 0.004 / 0.00004 of the squared box diagonal.  The reference draws its
+ * points from a private ISAAC context seeded with time(0) and the partners
+ * from libc random(); here both come from the caller's rc, so the estimate
+ * is reproducible.  Returns -1 on failure and NaN when clipping rejects
+ * more than 10 * ntries points, as the reference does. */
+double flam3gpu_dimension(flam3_genome *cp, int ntries, int clip_to_camera, randctx *rc) {
+  f3g_clear_error();
+  if (!rc) {
+    f3g_set_error("flam3gpu_dimension needs an ISAAC context");
+    return -1.0;
+  }
+  if (ntries < 2) ntries = 3000 * 1000;
+  double bmin[2], bmax[2];
+  if (clip_to_camera) {
+    const double scale = pow(2.0, cp->zoom), ppux = cp->pixels_per_unit * scale;
+    const double corner0 = cp->center[0] - cp->width / ppux / 2.0;
+    const double corner1 = cp->center[1] - cp->height / ppux / 2.0;
+    bmin[0] = corner0;
+    bmin[1] = corner1;
+    bmax[0] = corner0 + cp->width / ppux;
+    bmax[1] = corner1 + cp->height / ppux;
+  } else if (flam3gpu_estimate_bounding_box(cp, 0.0, 0, bmin, bmax, rc) < 0)
+    return -1.0;
+  const double d2max = (bmax[0] - bmin[0]) * (bmax[0] - bmin[0]) + (bmax[1] - bmin[1]) * (bmax[1] - bmin[1]);
+  const int sbs = 10000, maxchains = 64;
+  double *pts = (double *)malloc((size_t)ntries * 2 * sizeof(double));
+  double *buf = (double *)malloc((size_t)maxchains * sbs * 4 * sizeof(double));
+  double fd = -1.0;
+  if (!pts || !buf) {
+    f3g_set_error("host memory exhausted");
+    goto out;
+  }
+  long got = 0, nclipped = 0;
+  while (got < ntries) {
+    long need = ntries - got;
+    int nchains = (int)((need + sbs - 1) / sbs);
+    if (nchains > maxchains) nchains = maxchains;
+    long bv = 0;
+    if (chains_from_rc(cp, nchains, sbs, rc, buf, &bv)) goto out;
+    for (long i = 0; i < (long)nchains * sbs && got < ntries; i++) {
+      const double x = buf[4 * i], y = buf[4 * i + 1];
+      const int clipped = clip_to_camera && (x < bmin[0] || y < bmin[1] || x > bmax[0] || y > bmax[1]);
+      if (!clipped) {
+        pts[2 * got] = x;
+        pts[2 * got + 1] = y;
+        got++;
+      } else if (++nclipped > 10L * ntries) {
+        f3g_set_error("too much clipping, flam3gpu_dimension giving up");
+        fd = sqrt(-1.0);
+        goto out;
+      }
+    }
+  }
+  {
+    long n1 = 0, n2 = 0;
+    for (long i = 0; i < ntries; i++) {
+      long k;
+      /* the reference rejects the partner whose double index 2k equals i */
+      do {
+        k = (long)(f3g_irand(rc) % (unsigned long)ntries);
+      } while (2 * k == i);
+      const double dx = pts[2 * k] - pts[2 * i], dy = pts[2 * k + 1] - pts[2 * i + 1];
+      const double d2 = dx * dx + dy * dy;
+      if (d2 < 0.004 * d2max) n2++;
+      if (d2 < 0.00004 * d2max) n1++;
+    }
+    fd = 0.434294 * log(n2 / (n1 - 0.5));
+  }
+out:
+  free(pts);
+  free(buf);
+  return fd;
+}
+
+/* flam3_lyapunov (flam3.h:593, flam3.c:4054-4150): for each try a point is
+ * brought onto the attractor (one sample after 20 + (0..9) fuse steps),
+ * then one step is taken from it and one from a point eps = 1e-5 away in a
+ * random direction, and log(distance / eps) is averaged; the result is
+ * sum / (log 2 * ntries).  As in the reference the two steps draw their own
+ * random numbers (its ISAAC context advances between them), so they may
+ * pick different xforms.  All tries run as GPU chains in FP64; the draws
+ * come from the caller's rc (the reference: a private ISAAC context seeded
+ * with time(0), and libc random() for the fuse length). */
+double flam3gpu_lyapunov(flam3_genome *cp, int ntries, randctx *rc) {
+  f3g_clear_error();
+  if (!rc) {
+    f3g_set_error("flam3gpu_lyapunov needs an ISAAC context");
+    return -1.0;
+  }
+  if (ntries < 1) ntries = 10000;
+  const double eps = 1e-5;
+  double *st = (double *)malloc((size_t)ntries * 4 * sizeof(double));
+  double *on = (double *)malloc((size_t)ntries * 4 * sizeof(double));
+  double *s1 = (double *)malloc((size_t)ntries * 4 * sizeof(double));
+  double *s2 = (double *)malloc((size_t)ntries * 4 * sizeof(double));
+  double *tmp = (double *)malloc((size_t)ntries * 4 * sizeof(double));
+  int *fuse = (int *)malloc((size_t)ntries * sizeof(int));
+  long *idx = (long *)malloc((size_t)ntries * sizeof(long));
+  double res = -1.0;
+  long bv = 0;
+  if (!st || !on || !s1 || !s2 || !tmp || !fuse || !idx) {
+    f3g_set_error("host memory exhausted");
+    goto out;
+  }
+  for (int i = 0; i < ntries; i++) {
+    st[4 * i] = isaac_11(rc);
+    st[4 * i + 1] = isaac_11(rc);
+    st[4 * i + 2] = 0.0;
+    st[4 * i + 3] = 0.0;
+    fuse[i] = 20 + (int)(f3g_irand(rc) % 10);
+  }
+  /* onto the attractor: one chain per try, grouped by fuse length */
+  for (int f = 20; f < 30; f++) {
+    long cnt = 0;
+    for (int i = 0; i < ntries; i++)
+      if (fuse[i] == f) {
+        memcpy(tmp + 4 * cnt, st + 4 * i, 4 * sizeof(double));
+        idx[cnt++] = i;
+      }
+    if (!cnt) continue;
+    const uint64_t seed = (uint64_t)(uint32_t)f3g_irand(rc) | ((uint64_t)(uint32_t)f3g_irand(rc) << 32);
+    if (flam3gpu_iterate_chains(cp, (int)cnt, 1, f, tmp, seed, s1, &bv, 64)) goto out;
+    for (long c = 0; c < cnt; c++) memcpy(on + 4 * idx[c], s1 + 4 * c, 4 * sizeof(double));
+  }
+  /* one step from the point ... */
+  {
+    const uint64_t seed = (uint64_t)(uint32_t)f3g_irand(rc) | ((uint64_t)(uint32_t)f3g_irand(rc) << 32);
+    if (flam3gpu_iterate_chains(cp, ntries, 1, 0, on, seed, s1, &bv, 64)) goto out;
+  }
+  /* ... and one from a point eps away (flam3.c:4127-4137) */
+  for (int i = 0; i < ntries; i++) {
+    double dx, dy, r;
+    do {
+      dx = isaac_11(rc);
+      dy = isaac_11(rc);
+      r = sqrt(dx * dx + dy * dy);
+    } while (r == 0.0);
+    tmp[4 * i] = on[4 * i] + dx / r * eps;
+    tmp[4 * i + 1] = on[4 * i + 1] + dy / r * eps;
+    tmp[4 * i + 2] = 0.0;
+    tmp[4 * i + 3] = on[4 * i + 3];
+  }
+  {
+    const uint64_t seed = (uint64_t)(uint32_t)f3g_irand(rc) | ((uint64_t)(uint32_t)f3g_irand(rc) << 32);
+    if (flam3gpu_iterate_chains(cp, ntries, 1, 0, tmp, seed, s2, &bv, 64)) goto out;
+  }
+  {
+    double sum = 0.0;
+    for (int i = 0; i < ntries; i++) {
+      const double ex = s1[4 * i] - s2[4 * i], ey = s1[4 * i + 1] - s2[4 * i + 1];
+      sum += log(sqrt(ex * ex + ey * ey) / eps);
+    }
+    res = sum / (log(2.0) * ntries);
+  }
+out:
+  free(st);
+  free(on);
+  free(s1);
+  free(s2);
+  free(tmp);
+  free(fuse);
+  free(idx);
+  return res;
+}
+
+
+/* ---- strips (flam3-render.c:35-101, 311-345) ---- */
+
+int flam3gpu_calc_nstrips(flam3_frame *f, double budget_bytes) {
+  f3g_clear_error();
+  if (!f || f->ngenomes < 1) {
+    f3g_set_error("no genome");
+    return -1;
+  }
+  double avail = budget_bytes;
+  if (avail <= 0) {
+    size_t fr = 0, tot = 0;
+    if (!f3g_get_ctx() || cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+      f3g_set_error("no CUDA device available");
+      return -1;
+    }
+    avail = 0.8 * (double)fr;
+  }
+  const double need = flam3gpu_render_memory_required(f);
+  if (avail >= need) return 1;
+  return (int)ceil(need / avail);
+}
+
+int flam3gpu_render_strips(flam3_frame *f, void *out, int nchan, int transp, stat_struct *stats, int nstrips) {
+  f3g_clear_error();
+  if (!f || f->ngenomes < 1 || !out) {
+    f3g_set_error("no genome or output buffer");
+    return 1;
+  }
+  if (nstrips < 1) nstrips = 1;
+  const int real_height = f->genomes[0].height, width = f->genomes[0].width;
+  if (nstrips > real_height) {
+    f3g_set_error("cannot have more strips than rows but %d>%d", nstrips, real_height);
+    return 1;
+  }
+  /* per-strip copies of the genomes: top-level fields only change */
+  flam3_genome *orig = f->genomes;
+  flam3_genome *g = (flam3_genome *)malloc((size_t)f->ngenomes * sizeof(flam3_genome));
+  if (!g) {
+    f3g_set_error("host memory exhausted");
+    return 1;
+  }
+  const int strip_h = (int)ceil(real_height / (double)nstrips);
+  double *center_base = (double *)malloc((size_t)f->ngenomes * sizeof(double));
+  if (!center_base) {
+    free(g);
+    f3g_set_error("host memory exhausted");
+    return 1;
+  }
+  for (int k = 0; k < f->ngenomes; k++) {
+    const double zs = pow(2.0, orig[k].zoom);
+    center_base[k] = orig[k].center[1] - ((nstrips - 1) * strip_h) / (2 * orig[k].pixels_per_unit * zs);
+  }
+  const size_t row = (size_t)nchan * width * (f->bytes_per_channel == 2 ? 2 : 1);
+  randctx saved;
+  memcpy(&saved, &f->rc, sizeof(randctx));
+  stat_struct acc;
+  memset(&acc, 0, sizeof(acc));
+  int rv = 0;
+  for (int strip = 0; strip < nstrips && !rv; strip++) {
+    for (int k = 0; k < f->ngenomes; k++) {
+      g[k] = orig[k];
+      const double zs = pow(2.0, g[k].zoom);
+      g[k].sample_density *= nstrips;
+      g[k].height = strip_h;
+      g[k].center[1] = center_base[k] + strip_h * (double)strip / (g[k].pixels_per_unit * zs);
+      if (strip_h * (strip + 1) > real_height) {
+        g[k].height = real_height - strip_h * strip;
+        g[k].center[1] -= (strip_h - g[k].height) * 0.5 / (g[k].pixels_per_unit * zs);
+      }
+      g[k].ntemporal_samples = 1;
+    }
+    memcpy(&f->rc, &saved, sizeof(randctx));
+    f->genomes = g;
+    stat_struct st;
+    memset(&st, 0, sizeof(st));
+    rv = flam3gpu_render(f, (unsigned char *)out + (size_t)strip_h * strip * row, 0, nchan, transp, &st);
+    f->genomes = orig;
+    acc.num_iters += st.num_iters;
+    acc.badvals += st.badvals;
+    acc.render_seconds += st.render_seconds;
+  }
+  f->genomes = orig;
+  free(g);
+  free(center_base);
+  if (stats) *stats = acc;
+  return rv;
+}

@@ -50,6 +50,8 @@ def load():
     lib.flam3gpu_render_ex.argtypes = [F, C.c_void_p, C.c_int, C.c_int, C.c_int, S, C.POINTER(RenderIO)]
     lib.flam3gpu_render_memory_required.argtypes = [F]
     lib.flam3gpu_render_memory_required.restype = C.c_double
+    lib.flam3gpu_calc_nstrips.argtypes = [F, C.c_double]
+    lib.flam3gpu_render_strips.argtypes = [F, C.c_void_p, C.c_int, C.c_int, S, C.c_int]
     lib.flam3gpu_last_error.restype = C.c_char_p
     lib.flam3gpu_version.restype = C.c_char_p
     lib.flam3gpu_set_options.argtypes = [C.POINTER(Options)]
@@ -66,6 +68,10 @@ def load():
     lib.flam3gpu_interpolate.argtypes = [G, C.c_int, C.c_double, C.c_double, G]
     lib.flam3gpu_estimate_bounding_box.argtypes = [G, C.c_double, C.c_int, dp, dp, C.POINTER(abi.randctx)]
     lib.flam3gpu_colorhist.argtypes = [G, C.c_int, C.POINTER(abi.randctx), dp]
+    lib.flam3gpu_dimension.argtypes = [G, C.c_int, C.c_int, C.POINTER(abi.randctx)]
+    lib.flam3gpu_dimension.restype = C.c_double
+    lib.flam3gpu_lyapunov.argtypes = [G, C.c_int, C.POINTER(abi.randctx)]
+    lib.flam3gpu_lyapunov.restype = C.c_double
     lib.flam3gpu_free_genome.argtypes = [G]
     lib.flam3gpu_free_genome.restype = None
     lib.flam3gpu_set_interpolator.argtypes = [C.c_void_p]
@@ -126,6 +132,26 @@ def render(frame, field=0, nchan=3, transp=0, out=None, hist_in=None, want_hist=
 
 def memory_required(frame):
     return load().flam3gpu_render_memory_required(C.byref(frame.f))
+
+
+def calc_nstrips(frame, budget_bytes=0.0):
+    """calc_nstrips of flam3-render against device memory (or budget_bytes)."""
+    lib = load()
+    n = lib.flam3gpu_calc_nstrips(C.byref(frame.f), float(budget_bytes))
+    if n < 0:
+        _err(lib, "flam3gpu_calc_nstrips")
+    return n
+
+
+def render_strips(frame, nstrips, nchan=3, transp=0, out=None):
+    """flam3-render's strip loop on the GPU: (image, stats)."""
+    lib = load()
+    if out is None:
+        out = frame.out_buffer(nchan)
+    st = abi.stat_struct()
+    if lib.flam3gpu_render_strips(C.byref(frame.f), out.ctypes.data, nchan, transp, C.byref(st), nstrips):
+        _err(lib, "flam3gpu_render_strips")
+    return out, st
 
 
 def last_timings():
@@ -236,6 +262,34 @@ def estimate_bounding_box(genome, eps=0.01, nsamples=10000, rc=None):
     if bv < 0:
         _err(lib, "flam3gpu_estimate_bounding_box")
     return bmin, bmax, bv
+
+
+def dimension(genome, ntries=3000 * 1000, clip_to_camera=False, rc=None):
+    """flam3_dimension on the GPU: the correlation dimension estimate."""
+    lib = load()
+    from .isaac import init_rc
+    if rc is None:
+        rc = abi.randctx()
+        init_rc(rc, b"dimension")
+    g = getattr(genome, "g", genome)
+    d = lib.flam3gpu_dimension(C.byref(g), ntries, 1 if clip_to_camera else 0, C.byref(rc))
+    if d == -1.0:
+        _err(lib, "flam3gpu_dimension")
+    return d
+
+
+def lyapunov(genome, ntries=10000, rc=None):
+    """flam3_lyapunov on the GPU."""
+    lib = load()
+    from .isaac import init_rc
+    if rc is None:
+        rc = abi.randctx()
+        init_rc(rc, b"lyapunov")
+    g = getattr(genome, "g", genome)
+    v = lib.flam3gpu_lyapunov(C.byref(g), ntries, C.byref(rc))
+    if v == -1.0 and load().flam3gpu_last_error():
+        _err(lib, "flam3gpu_lyapunov")
+    return v
 
 
 def colorhist(genome, num_batches=10, rc=None):

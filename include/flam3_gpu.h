@@ -216,6 +216,27 @@ int flam3gpu_render(flam3_frame *f, void *out, int field, int nchan, int transp,
  * render of f->genomes[0] needs (histogram + accumulator + chain state). */
 double flam3gpu_render_memory_required(flam3_frame *f);
 
+/* Replaces calc_nstrips (flam3-render.c:35-101) for device memory: the number
+ * of horizontal strips the still f needs so that each strip's device bytes
+ * (flam3gpu_render_memory_required) fit budget_bytes, or 80 % of the free
+ * device memory when budget_bytes <= 0 (the reference: 80 % of physical host
+ * memory, or $use_mem).  Returns 1 when the whole image fits, -1 on failure. */
+int flam3gpu_calc_nstrips(flam3_frame *f, double budget_bytes);
+
+/* The strip loop of flam3-render (flam3-render.c:311-345) around
+ * flam3gpu_render: renders f (all fields, one temporal sample per genome, as
+ * flam3-render renders stills) in nstrips horizontal strips of
+ * ceil(height / nstrips) rows into the caller's full-size out buffer, each
+ * strip with sample_density * nstrips, its own centre and the same saved
+ * random context (f->rc is left as the last strip left it).  As in
+ * flam3-render, when the height is not a multiple of nstrips the strips are
+ * laid out for nstrips * ceil(height / nstrips) rows about the centre, which
+ * moves the image down by half the excess.  The caller's genomes are not
+ * modified.  stats receives the sums over the strips (each strip iterates
+ * the whole frame's samples, so nstrips times the plain render's).
+ * Returns 0 on success, 1 on failure (also when nstrips exceeds the height). */
+int flam3gpu_render_strips(flam3_frame *f, void *out, int nchan, int transp, stat_struct *stats, int nstrips);
+
 /* Last error message of the calling thread ("" if none). */
 const char *flam3gpu_last_error(void);
 

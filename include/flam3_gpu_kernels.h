@@ -80,6 +80,21 @@ int flam3gpu_estimate_bounding_box(flam3_genome *cp, double eps, int nsamples, d
  * 10000 samples after 20 fuse steps.  Returns 0 on success. */
 int flam3gpu_colorhist(flam3_genome *cp, int num_batches, randctx *rc, double *hist);
 
+/* flam3_dimension (flam3.h:592, flam3.c:3949-4052) on the GPU: the
+ * correlation dimension from ntries attractor points (optionally clipped to
+ * the camera) and ntries random pairs; same formula, defaults (ntries < 2:
+ * 3 000 000) and failure values (-1; NaN when clipping rejects more than
+ * 10 * ntries points).  Points and pair partners are drawn from rc (the
+ * reference: a private time-seeded ISAAC context and libc random()), so the
+ * estimate matches the reference's statistically. */
+double flam3gpu_dimension(flam3_genome *cp, int ntries, int clip_to_camera, randctx *rc);
+
+/* flam3_lyapunov (flam3.h:593, flam3.c:4054-4150) on the GPU: mean
+ * log2(distance / 1e-5) after one step from an attractor point and one from a
+ * point 1e-5 away, over ntries tries (ntries < 1: 10000), in FP64; draws
+ * from rc.  Returns -1 on failure. */
+double flam3gpu_lyapunov(flam3_genome *cp, int ntries, randctx *rc);
+
 /* flam3gpu_render without device allocation.  No counterpart in the
  * reference: for callers that cannot call cudaMalloc (inside CUDA-graph
  * construction, under a host-owned memory pool, with a fixed device-memory

@@ -134,3 +134,79 @@ def test_colorhist_matches_oracle_chains(gpulib):
     ho = np.bincount(np.clip((pts[:, 2] * 256).astype(int), 0, 255), minlength=256) / len(pts)
     assert abs(h.sum() - 1.0) < 1e-6
     assert np.abs(h - ho).sum() < 0.08, np.abs(h - ho).sum()
+
+
+def _sierpinski(width=512, height=512):
+    """three linear xforms of scale 1/2: the gasket on [0,1]^2, correlation
+    dimension log 3 / log 2"""
+    from flam3_gb300 import abi
+    G = gm.Genome(3)
+    for i, (tx, ty) in enumerate(((0.0, 0.0), (0.5, 0.0), (0.25, 0.5))):
+        x = G.xform(i)
+        x.c[0][0], x.c[0][1], x.c[1][0], x.c[1][1], x.c[2][0], x.c[2][1] = 0.5, 0.0, 0.0, 0.5, tx, ty
+        x.density = 1.0 / 3
+        x.color = i / 2.0
+        for j in range(abi.NVARS):
+            x.var[j] = 0.0
+        x.var[0] = 1.0
+    gm.resize(G, width, height)
+    G.g.center[0], G.g.center[1] = 0.5, 0.5
+    G.g.pixels_per_unit = width / 1.25  # the camera covers the gasket with a margin
+    G.g.zoom = 0.0
+    return G
+
+
+def _oracle_dimension(G, ntries, seed):
+    """flam3.c:3949-4052 restated on oracle chains (camera clip, no points
+    outside it for this genome)"""
+    rng = np.random.default_rng(seed)
+    nchains = (ntries + 9999) // 10000
+    starts = np.stack([rng.uniform(-1, 1, nchains), rng.uniform(-1, 1, nchains), np.zeros(nchains),
+                       np.zeros(nchains)], 1)
+    pts = _oracle.oracle_iterate_chains(G, starts, 10000, 20, int(rng.integers(1 << 62)))[0].reshape(-1, 4)
+    pts = pts[:ntries, :2]
+    span = G.g.width / G.g.pixels_per_unit, G.g.height / G.g.pixels_per_unit
+    d2max = span[0] ** 2 + span[1] ** 2
+    k = rng.integers(0, ntries, ntries)
+    d2 = np.sum((pts[k] - pts) ** 2, axis=1)
+    n2, n1 = np.sum(d2 < 0.004 * d2max), np.sum(d2 < 0.00004 * d2max)
+    return 0.434294 * np.log(n2 / (n1 - 0.5))
+
+
+def test_dimension_matches_oracle_and_theory(gpulib):
+    G = _sierpinski()
+    d = render.dimension(G, ntries=400000, clip_to_camera=True)
+    do = _oracle_dimension(G, 400000, 7)
+    assert abs(d - do) < 0.08, (d, do)
+    assert abs(d - np.log(3) / np.log(2)) < 0.15, d
+    # without the camera: the box comes from flam3_estimate_bounding_box
+    d2 = render.dimension(G, ntries=400000, clip_to_camera=False)
+    assert abs(d2 - np.log(3) / np.log(2)) < 0.2, d2
+
+
+def _oracle_lyapunov(G, ntries, seed):
+    """flam3.c:4054-4150 restated on oracle chains in FP64"""
+    rng = np.random.default_rng(seed)
+    st = np.stack([rng.uniform(-1, 1, ntries), rng.uniform(-1, 1, ntries), np.zeros(ntries), np.zeros(ntries)], 1)
+    on = _oracle.oracle_iterate_chains(G, st, 1, 25, int(rng.integers(1 << 62)))[0][:, 0]
+    s1 = _oracle.oracle_iterate_chains(G, on, 1, 0, int(rng.integers(1 << 62)))[0][:, 0]
+    ang = rng.uniform(0, 2 * np.pi, ntries)
+    pert = on.copy()
+    pert[:, 0] += 1e-5 * np.cos(ang)
+    pert[:, 1] += 1e-5 * np.sin(ang)
+    pert[:, 2] = 0.0
+    s2 = _oracle.oracle_iterate_chains(G, pert, 1, 0, int(rng.integers(1 << 62)))[0][:, 0]
+    r = np.hypot(s1[:, 0] - s2[:, 0], s1[:, 1] - s2[:, 1])
+    return np.sum(np.log(r / 1e-5)) / (np.log(2.0) * ntries)
+
+
+def test_lyapunov_matches_oracle(gpulib):
+    G = _sierpinski()
+    v = render.lyapunov(G, ntries=20000)
+    vo = _oracle_lyapunov(G, 20000, 3)
+    # the two steps draw independent xforms (as in the reference): 2/3 of the
+    # tries land a translation apart, 1/3 contract by 1/2
+    expect = ((2 / 3) * np.mean(np.log(np.array([0.5, 0.5590169943749475, 0.5590169943749475]) / 1e-5)) +
+              (1 / 3) * np.log(0.5))
+    assert abs(v - vo) < 0.3, (v, vo)
+    assert abs(v - expect / np.log(2.0)) < 0.5, (v, expect / np.log(2.0))

@@ -133,3 +133,40 @@ def test_animation_render_close_to_oracle(gpulib, t, nts, est, bits):
     g, sg = render.render(Fg)
     assert sg.num_iters == so.num_iters
     assert mae(o, g) < 2.5, mae(o, g)
+
+
+def test_calc_nstrips_against_budget(gpulib):
+    F = gm.Frame(gm.config0_genome(3), bits=33, seed="ns")
+    need = render.memory_required(F)
+    assert render.calc_nstrips(F, need * 10) == 1
+    assert render.calc_nstrips(F, need / 2.5) == 3
+    assert render.calc_nstrips(F) == 1  # a 512x512 still fits 80 % of free HBM
+
+
+def test_render_strips_matches_full_render(gpulib):
+    """flam3-render's strip loop: one strip is the plain render; three strips
+    (the last one shorter) carry the same image up to sampling noise, and the
+    caller's genome is unchanged."""
+    G = gm.config0_genome(4, width=200, height=250, quality=200.0)
+    F = gm.Frame(G, bits=33, seed="strips")
+    full, st_full = render.render(F)
+    F1 = gm.Frame(G, bits=33, seed="strips")
+    one, st_one = render.render_strips(F1, 1)
+    assert mae(full, one) < 0.02 and st_one.num_iters == st_full.num_iters
+    dens, cy, h = G.g.sample_density, G.g.center[1], G.g.height
+    F3 = gm.Frame(G, bits=33, seed="strips")
+    three, st3 = render.render_strips(F3, 3)
+    assert (G.g.sample_density, G.g.center[1], G.g.height) == (dens, cy, h)
+    # each strip iterates sample_density * 3 over a third of the rows: the
+    # full frame's samples per strip, three times in all (as flam3-render)
+    assert abs(st3.num_iters - 3 * st_full.num_iters) < 0.02 * 3 * st_full.num_iters
+    other, _ = render.render(gm.Frame(G, bits=33, seed="strips-other"))
+    noise = mae(full, other)
+    # flam3-render lays the strips out for 3 * 84 = 252 rows around the centre,
+    # which moves the 250-row image down by one row
+    assert mae(full[:-1], three[1:]) < 1.5 * noise + 0.05, (mae(full[:-1], three[1:]), noise)
+    # every strip is populated (no empty band at a seam)
+    for r0 in (0, 84, 168):
+        assert three[r0 + 1:r0 + 82].mean() > 0.5 * full[r0:r0 + 81].mean()
+    with pytest.raises(render.Flam3GpuError):
+        render.render_strips(gm.Frame(G, bits=33, seed="x"), 251)
