@@ -58,6 +58,9 @@ CPU_QUALITY = 100.0  # bounded CPU sample: same genome and size at quality 100 (
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none \
 #       -k "regex:k_iterate|k_de_tile" -c 2 <one config-1 render>   (1 pass)
 ITERATE_TRAFFIC = 26.14e6 + 1.47e6    # k_iterate: bucket atomics resolve in L2
+# k_iterate warp instructions per plotted sample (ncu smsp__inst_executed.sum
+# / plotted samples on the 960x540 q2000 config-1 case)
+ITERATE_WARP_INSTR_PER_SAMPLE = 20.0
 TAIL_TRAFFIC = 136.54e6 + 3.54e6      # k_de_tile: the histogram once, part of the image
 
 
@@ -261,6 +264,25 @@ def run_gpu(args):
                  "frac": nd_bytes / t_nd / 1e9 / hbm_peak, "traffic": None, "ms": t_nd * 1e3,
                  "note": f"config-1 genome and size with estimator 0: histogram {hist_bytes / 1e6:.1f} MB read + "
                          f"image {out_bytes / 1e6:.1f} MB write; peak {peak_kind}; L2 flushed before each render"}
+    # the iterate kernel's own ceilings: the measured L2 float4-atomic rate at
+    # random buckets of this histogram (one add per plotted sample) and the
+    # issue rate over the instructions a sample takes
+    ceilings = None
+    if world == 1:
+        plotted_per_s = plotted / it_s
+        atom = render.measure_atomic_rate(d["w"] * d["h"], 1 << 31)
+        sm_mhz = (clk.summary() or {}).get("sm_mhz") or 2070.0
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+        issue_peak = nsm * 4 * sm_mhz * 1e6
+        ceil_issue = issue_peak / ITERATE_WARP_INSTR_PER_SAMPLE
+        ceilings = {
+            "achieved_samples_per_s": plotted_per_s,
+            "l2_atomic": {"measured_adds_per_s": atom, "frac": plotted_per_s / atom,
+                          "note": "float4 atomic adds at random buckets of the config-1 histogram, every SM"},
+            "issue": {"warp_instr_per_sample": ITERATE_WARP_INSTR_PER_SAMPLE, "peak_warp_instr_per_s": issue_peak,
+                      "ceiling_samples_per_s": ceil_issue, "frac": plotted_per_s / ceil_issue,
+                      "note": f"{nsm} SMs x 4 schedulers x {sm_mhz:.0f} MHz; instructions per sample from ncu"},
+        }
     cb = None
     if world == 1 and not args.no_cpu:
         cb, _ = cpu_baseline(steps=1)
@@ -275,7 +297,8 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "kernel": "k_iterate", "achieved": it_gbs, "peak": hbm_peak,
                      "unit": "GB/s", "frac": it_gbs / hbm_peak, "traffic": ITERATE_TRAFFIC,
                      "note": f"16 B bucket RMW per plotted sample ({plotted / args.steps / 1e9:.3f} G/render); "
-                             f"peak {peak_kind}; the kernel is issue/latency bound, not HBM bound"},
+                             f"peak {peak_kind}; the kernel is issue/latency bound, not HBM bound",
+                     "ceilings": ceilings},
         "roofline_tail": {"bound": "hbm", "kernel": "DE + filter + tonemap", "achieved": tail_gbs,
                           "peak": hbm_peak, "unit": "GB/s",
                           "frac": (tail_gbs / hbm_peak) if tail_gbs else None, "traffic": TAIL_TRAFFIC,

@@ -56,6 +56,10 @@ int f3g_launch_de_fused_tile(const void *buckets, int bkind, const void *count, 
 /* raises the tail kernels' shared-memory limits (call before stream capture) */
 int f3g_de_prepare(void);
 int f3g_tail_prepare(void);
+/* ceiling probe: blocks x 256 threads each add per_thread float4s at
+ * pseudo-random buckets of buf[nbuckets] (f3g_probe.cu) */
+int f3g_launch_atomic_rate(float4 *buf, unsigned long long nbuckets, int blocks, int per_thread, uint32_t salt,
+                           cudaStream_t st);
 /* separable strip kernels (f3g_strip_{f32,f64}{,e}.cu: FP32/FP64
  * histogram, earlyclip off/on): -2 when no instantiation covers
  * (oversample, fw) */

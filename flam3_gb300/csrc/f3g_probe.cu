@@ -51,3 +51,30 @@ extern "C" int f3g_launch_iterate_chains(const F3GPass *d_pass, int nchains, int
   }
   return (int)cudaGetLastError();
 }
+
+/* ---------------------------------------------------------------------
+ * Ceiling probe for the iterate kernel's roofline: float4 atomic adds
+ * (red.global.add.v4.f32, the bucket update of plot()) at pseudo-random
+ * buckets of a histogram-sized buffer, every lane its own bucket.
+ * ------------------------------------------------------------------- */
+namespace f3g {
+__global__ void __launch_bounds__(256) k_atomic_rate(float4 *buf, unsigned long long nbuckets, int per_thread,
+                                                     uint32_t salt) {
+  uint32_t h = (blockIdx.x * blockDim.x + threadIdx.x) * 0x9E3779B1u ^ salt;
+  const float4 one = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+  for (int i = 0; i < per_thread; i++) {
+    /* xorshift32: a new bucket per add */
+    h ^= h << 13;
+    h ^= h >> 17;
+    h ^= h << 5;
+    const unsigned long long b = (unsigned long long)h * nbuckets >> 32;
+    atomicAdd(buf + b, one);
+  }
+}
+}  // namespace f3g
+
+extern "C" int f3g_launch_atomic_rate(float4 *buf, unsigned long long nbuckets, int blocks, int per_thread,
+                                      uint32_t salt, cudaStream_t st) {
+  f3g::k_atomic_rate<<<blocks, 256, 0, st>>>(buf, nbuckets, per_thread, salt);
+  return (int)cudaGetLastError();
+}

@@ -580,3 +580,45 @@ int flam3gpu_render_strips(flam3_frame *f, void *out, int nchan, int transp, sta
   if (stats) *stats = acc;
   return rv;
 }
+
+/* ---- ceiling probe for the iterate roofline ---- */
+
+int flam3gpu_measure_atomic_rate(long long nbuckets, long long natomics, double *per_second) {
+  f3g_clear_error();
+  f3g_ctx *c = f3g_get_ctx();
+  if (!c || nbuckets <= 0 || natomics <= 0 || !per_second) {
+    f3g_set_error(c ? "bad arguments" : "no CUDA device available");
+    return 1;
+  }
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = (nsm > 0 ? nsm : 1) * 8;
+  long long per = natomics / ((long long)blocks * 256);
+  if (per < 1) per = 1;
+  if (per > (1 << 30)) per = 1 << 30;
+  float4 *buf = NULL;
+  cudaEvent_t e0 = NULL, e1 = NULL;
+  int rv = 1;
+  if (cudaMalloc((void **)&buf, (size_t)nbuckets * sizeof(float4)) != cudaSuccess) goto out;
+  if (cudaMemsetAsync(buf, 0, (size_t)nbuckets * sizeof(float4), c->stream) != cudaSuccess) goto out;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) goto out;
+  /* one warm-up launch, then the timed one */
+  if (f3g_launch_atomic_rate(buf, (unsigned long long)nbuckets, blocks, (int)(per / 8 + 1), 1u, c->stream)) goto out;
+  cudaEventRecord(e0, c->stream);
+  if (f3g_launch_atomic_rate(buf, (unsigned long long)nbuckets, blocks, (int)per, 2u, c->stream)) goto out;
+  cudaEventRecord(e1, c->stream);
+  if (cudaEventSynchronize(e1) != cudaSuccess) goto out;
+  {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    *per_second = (double)blocks * 256 * per / (ms / 1e3);
+  }
+  rv = 0;
+out:
+  if (rv && !flam3gpu_last_error()[0]) f3g_set_error("CUDA error: %s", cudaGetErrorString(cudaGetLastError()));
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(buf);
+  return rv;
+}

@@ -68,6 +68,7 @@ def load():
     lib.flam3gpu_interpolate.argtypes = [G, C.c_int, C.c_double, C.c_double, G]
     lib.flam3gpu_estimate_bounding_box.argtypes = [G, C.c_double, C.c_int, dp, dp, C.POINTER(abi.randctx)]
     lib.flam3gpu_colorhist.argtypes = [G, C.c_int, C.POINTER(abi.randctx), dp]
+    lib.flam3gpu_measure_atomic_rate.argtypes = [C.c_longlong, C.c_longlong, dp]
     lib.flam3gpu_dimension.argtypes = [G, C.c_int, C.c_int, C.POINTER(abi.randctx)]
     lib.flam3gpu_dimension.restype = C.c_double
     lib.flam3gpu_lyapunov.argtypes = [G, C.c_int, C.POINTER(abi.randctx)]
@@ -290,6 +291,15 @@ def lyapunov(genome, ntries=10000, rc=None):
     if v == -1.0 and load().flam3gpu_last_error():
         _err(lib, "flam3gpu_lyapunov")
     return v
+
+
+def measure_atomic_rate(nbuckets, natomics=1 << 31):
+    """float4 atomic adds per second at random buckets (roofline ceiling)."""
+    lib = load()
+    r = C.c_double()
+    if lib.flam3gpu_measure_atomic_rate(int(nbuckets), int(natomics), C.byref(r)):
+        _err(lib, "flam3gpu_measure_atomic_rate")
+    return r.value
 
 
 def colorhist(genome, num_batches=10, rc=None):

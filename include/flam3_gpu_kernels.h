@@ -95,6 +95,12 @@ double flam3gpu_dimension(flam3_genome *cp, int ntries, int clip_to_camera, rand
  * from rc.  Returns -1 on failure. */
 double flam3gpu_lyapunov(flam3_genome *cp, int ntries, randctx *rc);
 
+/* Ceiling probe (no counterpart in the reference): float4 atomic adds per
+ * second at pseudo-random buckets of an nbuckets histogram, natomics adds in
+ * one timed launch over every SM; the bucket update of the chaos game is one
+ * such add per plotted sample.  Returns 0 on success. */
+int flam3gpu_measure_atomic_rate(long long nbuckets, long long natomics, double *per_second);
+
 /* flam3gpu_render without device allocation.  No counterpart in the
  * reference: for callers that cannot call cudaMalloc (inside CUDA-graph
  * construction, under a host-owned memory pool, with a fixed device-memory

@@ -210,3 +210,9 @@ def test_lyapunov_matches_oracle(gpulib):
               (1 / 3) * np.log(0.5))
     assert abs(v - vo) < 0.3, (v, vo)
     assert abs(v - expect / np.log(2.0)) < 0.5, (v, expect / np.log(2.0))
+
+
+def test_atomic_rate_probe(gpulib):
+    """the roofline probe runs and reports a plausible L2 float4-atomic rate"""
+    r = render.measure_atomic_rate(1 << 20, 1 << 26)
+    assert 1e9 < r < 1e13, r
