@@ -64,3 +64,29 @@ def test_service_config_defaults_without_gpu():
     c = service.config(round_samples=-1, streams=3)
     assert c.round_samples == -1 and c.streams == 3
 
+
+
+def test_strip_planning_without_gpu():
+    """calc_nstrips against a given budget and the strip loop's argument
+    checks are host logic (flam3-render.c:35-101, 276-283)"""
+    from flam3_gb300 import genome as gm, render
+
+    F = gm.Frame(gm.config0_genome(3, width=64, height=40), bits=33, seed="s")
+    need = render.memory_required(F)
+    assert need > 0
+    assert render.calc_nstrips(F, need) == 1
+    assert render.calc_nstrips(F, need / 3.5) == 4
+    with pytest.raises(render.Flam3GpuError, match="more strips than rows"):
+        render.render_strips(F, 41)
+
+
+def test_analysis_helpers_need_a_random_context():
+    """flam3gpu_dimension / flam3gpu_lyapunov refuse a NULL context before
+    touching the device"""
+    from flam3_gb300 import genome as gm, render
+
+    lib = render.load()
+    G = gm.config0_genome(3)
+    assert lib.flam3gpu_dimension(C.byref(G.g), 1000, 0, None) == -1.0
+    assert b"ISAAC" in lib.flam3gpu_last_error()
+    assert lib.flam3gpu_lyapunov(C.byref(G.g), 10, None) == -1.0
