@@ -21,6 +21,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#include <unistd.h>
 
 #include "f3g_host.h"
 
@@ -310,10 +311,56 @@ fail:
   f3g_genome_free(&cp);
 }
 
-static void *pass_worker(void *arg) {
-  const pass_job *pj = (const pass_job *)arg;
-  for (int ts = pj->start; ts < pj->ntemporal; ts += pj->stride) build_one_pass(pj, ts);
+/* Process-wide planning workers: the temporal samples of every concurrent
+ * f3g_build_batch_passes call are handed out one at a time (the calling
+ * thread works on its own call too), so no threads are created per frame
+ * and uneven samples balance themselves.  Workers start on first use (up to
+ * 16, one per online core but the caller's) and live for the process. */
+typedef struct plan_batch_s {
+  const pass_job *pj;
+  int next, done, n;
+  struct plan_batch_s *link;
+} plan_batch;
+
+static pthread_mutex_t pl_mu = PTHREAD_MUTEX_INITIALIZER;
+static pthread_cond_t pl_work = PTHREAD_COND_INITIALIZER, pl_done = PTHREAD_COND_INITIALIZER;
+static plan_batch *pl_head = NULL;
+static int pl_workers = 0;
+
+static void *plan_worker(void *arg) {
+  (void)arg;
+  pthread_mutex_lock(&pl_mu);
+  for (;;) {
+    plan_batch *b = pl_head;
+    while (b && b->next >= b->n) b = b->link;
+    if (!b) {
+      pthread_cond_wait(&pl_work, &pl_mu);
+      continue;
+    }
+    const int ts = b->next++;
+    pthread_mutex_unlock(&pl_mu);
+    build_one_pass(b->pj, ts);
+    pthread_mutex_lock(&pl_mu);
+    if (++b->done == b->n) pthread_cond_broadcast(&pl_done);
+  }
   return NULL;
+}
+
+/* under pl_mu */
+static void plan_workers_start(void) {
+  long ncpu = sysconf(_SC_NPROCESSORS_ONLN);
+  int want = (int)(ncpu > 1 ? ncpu - 1 : 0);
+  if (want > 16) want = 16;
+  while (pl_workers < want) {
+    pthread_t th;
+    pthread_attr_t at;
+    pthread_attr_init(&at);
+    pthread_attr_setdetachstate(&at, PTHREAD_CREATE_DETACHED);
+    const int ok = pthread_create(&th, &at, plan_worker, NULL) == 0;
+    pthread_attr_destroy(&at);
+    if (!ok) break;
+    pl_workers++;
+  }
 }
 
 int f3g_build_batch_passes(flam3_frame *spec, int field, const f3g_geom *g, int batch, int nbatches, int ntemporal,
@@ -321,25 +368,31 @@ int f3g_build_batch_passes(flam3_frame *spec, int field, const f3g_geom *g, int 
                            f3g_pass_info *info) {
   /* keys in order: the caller's ISAAC context advances as the reference's */
   for (int ts = 0; ts < ntemporal; ts++) consume_rc(spec, passes[ts].key);
-  int nt = ntemporal / 4;
-  if (nt > 16) nt = 16;
-  if (nt < 1) nt = 1;
   pass_job pj = {spec, g, field, batch * ntemporal, ntemporal, nbatches, cmap_size, 1, 0, tfilter, tdeltas, passes, info};
-  if (nt == 1) {
-    pass_worker(&pj);
+  if (ntemporal < 3) {
+    for (int ts = 0; ts < ntemporal; ts++) build_one_pass(&pj, ts);
   } else {
-    pthread_t th[16];
-    pass_job jobs[16];
-    int started[16];
-    for (int k = 0; k < nt; k++) {
-      jobs[k] = pj;
-      jobs[k].stride = nt;
-      jobs[k].start = k;
-      started[k] = pthread_create(&th[k], NULL, pass_worker, &jobs[k]) == 0;
-      if (!started[k]) pass_worker(&jobs[k]);
+    plan_batch b = {&pj, 0, 0, ntemporal, NULL};
+    pthread_mutex_lock(&pl_mu);
+    plan_workers_start();
+    plan_batch **tail = &pl_head;
+    while (*tail) tail = &(*tail)->link;
+    *tail = &b;
+    pthread_cond_broadcast(&pl_work);
+    while (b.next < b.n) {
+      const int ts = b.next++;
+      pthread_mutex_unlock(&pl_mu);
+      build_one_pass(&pj, ts);
+      pthread_mutex_lock(&pl_mu);
+      b.done++;
     }
-    for (int k = 0; k < nt; k++)
-      if (started[k]) pthread_join(th[k], NULL);
+    while (b.done < b.n) pthread_cond_wait(&pl_done, &pl_mu);
+    for (plan_batch **q = &pl_head; *q; q = &(*q)->link)
+      if (*q == &b) {
+        *q = b.link;
+        break;
+      }
+    pthread_mutex_unlock(&pl_mu);
   }
   for (int ts = 0; ts < ntemporal; ts++)
     if (info[ts].err) {
