@@ -149,9 +149,17 @@ def cpu_baseline(steps=1, quality=CPU_QUALITY):
         times.append(time.perf_counter() - t0)
         iters = st.num_iters
     val = iters / statistics.median(times) / 1e9
+    # the single-thread row: the same render at a tenth of the quality
+    G = gm.config1_genome(1, quality=quality / 10)
+    F = gm.Frame(G, bits=33, nthreads=1, seed="cpu-1t")
+    t0 = time.perf_counter()
+    _, st1, _ = _oracle.oracle_render(F, fast=True)
+    one = st1.num_iters / (time.perf_counter() - t0) / 1e9
     return {"value": val, "unit": "Giter/s", "cores": nt, "kind": "port",
+            "single_thread_value": one,
             "sample": f"same genome and 1920x1080 ss2 DE9 render at quality {quality:g} "
-                      f"({iters / 1e6:.0f} M iterations) per step, median of {steps}"}, times
+                      f"({iters / 1e6:.0f} M iterations) per step, median of {steps}; single thread: quality "
+                      f"{quality / 10:g} ({st1.num_iters / 1e6:.0f} M iterations)"}, times
 
 
 def run_reference(args):
