@@ -5,7 +5,7 @@ genome with 2-4 variations each from variations 0-19, 1920x1080 output,
 quality 2000, supersample 2 (a 3878x2198 histogram incl. gutter), density
 estimation radius 9, gaussian filter radius 1, bits=33 -- 4.147 G chaos-game
 iterations, then DE + spatial filter + tonemap.  Inputs are synthetic: the
-genome comes from a seeded generator (flam3_gb300.genome.config1_genome).
+genome comes from a seeded generator (flam3_gb300.genome.still_genome).
 
   value  Giter/s with the genome already on the device side of the call:
          iterations / (sum of the render's kernel times, CUDA events on the
@@ -21,13 +21,13 @@ genome comes from a seeded generator (flam3_gb300.genome.config1_genome).
 The same line carries the batched and served legs of the metric
 ("renders/s and p50/p99 latency, served vs plain"):
 
-  batched_animation  config 2: two 5-xform genomes interpolated over 120
+  batched_animation  two 5-xform genomes interpolated over 120
          frames of 1280x720 q500, 100 temporal samples, DE r7; the plain
          drop-in frame after frame vs flam3gpu_render_batch (one persistent
          launch over all frames and temporal samples, graph-captured tails)
-  batched_mixed      config 3: 256 mixed-size jobs, plain one at a time vs
+  batched_mixed      256 mixed-size jobs, plain one at a time vs
          one batch
-  served             config 4: a Poisson trace (95% config-3 jobs, 5%
+  served             a Poisson trace (95% mixed-size jobs, 5%
          3840x2160 q1000 ss2 DE11); renders/s at saturation and p50/p95/p99
          latency at one arrival rate, plain (one request at a time) vs the
          render service (continuous batching); plus the mean absolute
@@ -52,14 +52,14 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC = "Giter/s; renders/s and p50/p99 latency, served vs plain, at matched image error"
-WORKLOAD = "config1 still: 1920x1080 q2000 ss2 DE r9 gaussian r1, 6 xforms + final, bits 33"
+WORKLOAD = "still: 1920x1080 q2000 ss2 DE r9 gaussian r1, 6 xforms + final, bits 33"
 CPU_QUALITY = 100.0  # bounded CPU sample: same genome and size at quality 100 (1/20 of the iterations)
-# DRAM bytes (read + write) per launch on one full config-1 render, from
+# DRAM bytes (read + write) per launch on one full 1920x1080 q2000 still render, from
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none \
-#       -k "regex:k_iterate|k_de_tile" -c 2 <one config-1 render>   (1 pass)
+#       -k "regex:k_iterate|k_de_tile" -c 2 <one still render>   (1 pass)
 ITERATE_TRAFFIC = 26.14e6 + 1.47e6    # k_iterate: bucket atomics resolve in L2
 # k_iterate warp instructions per plotted sample (ncu smsp__inst_executed.sum
-# / plotted samples on the 960x540 q2000 config-1 case)
+# / plotted samples on the 960x540 q2000 case of the same genome)
 ITERATE_WARP_INSTR_PER_SAMPLE = 20.0
 TAIL_TRAFFIC = 136.54e6 + 3.54e6      # k_de_tile: the histogram once, part of the image
 
@@ -142,7 +142,7 @@ def cpu_baseline(steps=1, quality=CPU_QUALITY):
     nt = cpu_threads()
     times, iters = [], 0
     for s in range(steps):
-        G = gm.config1_genome(1, quality=quality)
+        G = gm.still_genome(1, quality=quality)
         F = gm.Frame(G, bits=33, nthreads=nt, seed="cpu-%d" % s)
         t0 = time.perf_counter()
         out, st, _ = _oracle.oracle_render(F, fast=True)
@@ -150,7 +150,7 @@ def cpu_baseline(steps=1, quality=CPU_QUALITY):
         iters = st.num_iters
     val = iters / statistics.median(times) / 1e9
     # the single-thread row: the same render at a tenth of the quality
-    G = gm.config1_genome(1, quality=quality / 10)
+    G = gm.still_genome(1, quality=quality / 10)
     F = gm.Frame(G, bits=33, nthreads=1, seed="cpu-1t")
     t0 = time.perf_counter()
     _, st1, _ = _oracle.oracle_render(F, fast=True)
@@ -216,7 +216,7 @@ def run_gpu(args):
         _build.build()
     render.load()
     hbm_peak, peak_kind = peaks()
-    G = gm.config1_genome(1)
+    G = gm.still_genome(1)
     flush = torch.empty(320 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def one(seed):
@@ -259,7 +259,7 @@ def run_gpu(args):
     # log-scale + filter + tonemap + pack kernel, an HBM-streaming pass
     nodde = None
     if world == 1:
-        Gn = gm.config1_genome(1, estimator=0.0)
+        Gn = gm.still_genome(1, estimator=0.0)
         tails = []
         for s_ in range(args.warmup + args.steps):
             flush_l2(flush)
@@ -270,7 +270,7 @@ def run_gpu(args):
         nodde = {"bound": "hbm", "kernel": "k_log_filter_strip (log scale + separable filter + tonemap + pack, no DE)",
                  "achieved": nd_bytes / t_nd / 1e9, "peak": hbm_peak, "unit": "GB/s",
                  "frac": nd_bytes / t_nd / 1e9 / hbm_peak, "traffic": None, "ms": t_nd * 1e3,
-                 "note": f"config-1 genome and size with estimator 0: histogram {hist_bytes / 1e6:.1f} MB read + "
+                 "note": f"the still genome and size with estimator 0: histogram {hist_bytes / 1e6:.1f} MB read + "
                          f"image {out_bytes / 1e6:.1f} MB write; peak {peak_kind}; L2 flushed before each render"}
     # the iterate kernel's own ceilings: the measured L2 float4-atomic rate at
     # random buckets of this histogram (one add per plotted sample) and the
@@ -292,7 +292,7 @@ def run_gpu(args):
             "l2_atomic": {"measured_adds_per_s": atom, "frac": plotted_per_s / atom,
                           "full_histogram_adds_per_s": atom_full,
                           "note": "float4 atomic adds at random buckets of a 16 MB (L2-resident) histogram, every "
-                                  "SM; full_histogram: over the config-1 histogram's 136 MB"},
+                                  "SM; full_histogram: over the still's 136 MB histogram"},
             "issue": {"warp_instr_per_sample": ITERATE_WARP_INSTR_PER_SAMPLE, "peak_warp_instr_per_s": issue_peak,
                       "ceiling_samples_per_s": ceil_issue, "frac": plotted_per_s / ceil_issue,
                       "note": f"{nsm} SMs x 4 schedulers x {sm_mhz:.0f} MHz; instructions per sample from ncu"},
@@ -380,12 +380,12 @@ def leg_batched(name, make_frames, note):
 
 
 def leg_served(nreq, seed=4, ref_check=3):
-    """config 4 trace: saturation throughput and latency at one arrival rate"""
+    """serving trace: saturation throughput and latency at one arrival rate"""
     import numpy as np
     from flam3_gb300 import genome as gm, render, service
 
     def trace(rate):
-        tr = gm.config4_trace(seed=seed, nrequests=nreq, rate_hz=rate)
+        tr = gm.serving_trace(seed=seed, nrequests=nreq, rate_hz=rate)
         return [(t, gm.Frame(G, bits=b, seed="srv-%d" % i)) for i, (t, G, b) in enumerate(tr)]
 
     # saturation: every request queued at t=0
@@ -443,7 +443,7 @@ def leg_served(nreq, seed=4, ref_check=3):
         errs.append({"request": i, "mae_plain": mae(plain_imgs[i], hq) / 255.0,
                      "mae_served": mae(served_imgs[i], hq) / 255.0})
     q = lambda xs: {"p50": 1e3 * pct(xs, 50), "p95": 1e3 * pct(xs, 95), "p99": 1e3 * pct(xs, 99)}
-    return {"workload": "config4 trace: %d requests, 95%% config-3 jobs, 5%% 3840x2160 q1000 ss2 DE11" % nreq,
+    return {"workload": "serving trace: %d requests, 95%% mixed-size jobs, 5%% 3840x2160 q1000 ss2 DE11" % nreq,
             "plain_renders_per_s": cap_plain, "served_renders_per_s": nreq / t_served,
             "plain_device_s": {k.replace("_ms", "_s"): v / 1e3 for k, v in dev.items()},
             "speedup": t_plain / t_served, "rate_hz": rate,
@@ -458,21 +458,23 @@ def run_legs(args):
     from flam3_gb300 import genome as gm
 
     out = {}
-    if "c2" in args.legs:
-        def c2(tag):
-            gs = gm.config2_genomes(2)
-            return [gm.Frame(gs, bits=33, seed="c2-%s-%d" % (tag, i), time=float(i)) for i in range(args.c2_frames)]
+    legs = args.legs.split(",") if args.legs else []
+    if "animation" in legs:
+        def frames(tag):
+            gs = gm.animation_keys(2)
+            return [gm.Frame(gs, bits=33, seed="anim-%s-%d" % (tag, i), time=float(i))
+                    for i in range(args.animation_frames)]
 
-        out["batched_animation"] = leg_batched("c2", c2, "config2: %d frames 1280x720 q500 100 temporal samples DE7"
-                                               % args.c2_frames)
-    if "c3" in args.legs:
-        def c3(tag):
-            return [gm.Frame(G, bits=b, seed="c3-%s-%d" % (tag, i))
-                    for i, (G, b) in enumerate(gm.config3_jobs(3, njobs=args.c3_jobs))]
+        out["batched_animation"] = leg_batched("animation", frames, "animation: %d frames 1280x720 q500 100 "
+                                               "temporal samples DE7" % args.animation_frames)
+    if "mixed" in legs:
+        def jobs(tag):
+            return [gm.Frame(G, bits=b, seed="mixed-%s-%d" % (tag, i))
+                    for i, (G, b) in enumerate(gm.mixed_jobs(3, njobs=args.mixed_jobs))]
 
-        out["batched_mixed"] = leg_batched("c3", c3, "config3: %d mixed jobs" % args.c3_jobs)
-    if "c4" in args.legs:
-        out["served"] = leg_served(args.c4_requests)
+        out["batched_mixed"] = leg_batched("mixed", jobs, "mixed: %d jobs" % args.mixed_jobs)
+    if "served" in legs:
+        out["served"] = leg_served(args.served_requests)
     return out
 
 
@@ -483,10 +485,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--legs", default="c2,c3,c4", help="batched/served legs to add (c2,c3,c4; empty: none)")
-    ap.add_argument("--c2-frames", type=int, default=120)
-    ap.add_argument("--c3-jobs", type=int, default=256)
-    ap.add_argument("--c4-requests", type=int, default=64)
+    ap.add_argument("--legs", default="animation,mixed,served",
+                    help="batched/served legs to add (animation,mixed,served; empty: none)")
+    ap.add_argument("--animation-frames", type=int, default=120)
+    ap.add_argument("--mixed-jobs", type=int, default=256)
+    ap.add_argument("--served-requests", type=int, default=64)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

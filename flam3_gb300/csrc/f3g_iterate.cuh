@@ -33,7 +33,7 @@
 namespace f3g {
 
 /* F3G_FINAL_UNROLL: 1 (default) gives the final xform its own apply_xform
- * call site (more code, fewer loop branches: 4 % faster on the config-1
+ * call site (more code, fewer loop branches: 4 % faster on the 1920x1080
  * still); 0 shares one site */
 #ifndef F3G_FINAL_UNROLL
 #define F3G_FINAL_UNROLL 1
@@ -309,10 +309,10 @@ __device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, int S
 /* F3G_AGG: 0 never aggregate bucket adds, 1 (default) always for FP64
  * buckets (four atomics per sample) and, for FP32 buckets, per chunk when
  * probes taken right after block shuffles find at least F3G_AGG_LANES of a
- * warp's points sharing buckets, 2 always.  Measured on the config-1 still /
- * a config-2 key genome whose attractor covers few buckets: never 45.9 /
+ * warp's points sharing buckets, 2 always.  Measured on the 1920x1080 q2000 still /
+ * an animation key genome whose attractor covers few buckets: never 45.9 /
  * 10.0 Giter/s, always 38.0 / 41.0, probed after the shuffle with 8 lanes
- * 48.7 / 39.2 (the config-1 chunks stay direct); FP64 buckets 13.9 without,
+ * 48.7 / 39.2 (the still's chunks stay direct); FP64 buckets 13.9 without,
  * 20.2 with aggregation. */
 #ifndef F3G_AGG
 #define F3G_AGG 1
@@ -323,7 +323,7 @@ __device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, int S
 
 /* F3G_SHUF_WARPS: warps per shuffle group (8 = the whole block, default);
  * smaller groups synchronise on named barriers and wait for fewer warps, but
- * mix less: measured on the config-1 still, groups of 4 warps 43.2 Giter/s
+ * mix less: measured on the 1920x1080 still, groups of 4 warps 43.2 Giter/s
  * and 0.4 % more image error than whole-block shuffles at 49.4 */
 #ifndef F3G_SHUF_WARPS
 #define F3G_SHUF_WARPS 8

@@ -6,7 +6,7 @@ flam3_defaults_on (flam3.c:1270-1370) and initialize_xforms
 (variations.c:2401-2563).  `Frame` wraps a flam3_frame over a list of
 genomes with the ISAAC context seeded as flam3_init_frame does.
 
-The seeded generators `config0_genome` ... `config4_trace` build the
+The seeded generators `small_genome` ... `serving_trace` build the
 synthetic workloads (3 xforms linear/sinusoidal/spherical; 6+final xforms
 drawn from variations 0-19; interpolated animations; mixed-size batches).
 Their camera rule: center on the bounding box of a short chaos game
@@ -322,7 +322,7 @@ def resize(genome, width, height):
     g.height = height
 
 
-CONFIG1_VARIATIONS = list(range(20))
+VARIATIONS_0_19 = list(range(20))
 
 
 def _render_params(g, width, height, quality, oversample, estimator, filter_radius):
@@ -342,7 +342,7 @@ def _render_params(g, width, height, quality, oversample, estimator, filter_radi
     g.nbatches = 1
 
 
-def config0_genome(seed=0, width=512, height=512, quality=50.0):
+def small_genome(seed=0, width=512, height=512, quality=50.0):
     """3 xforms, coefs U(-1,1), weights U(.2,1) normalised, color U(0,1),
     color_speed .5, linear .5 / sinusoidal .3 / spherical .2, 8-colour
     gradient palette; 512x512 q50 ss1, no DE, gaussian r=0.5, gamma 4,
@@ -368,7 +368,7 @@ def config0_genome(seed=0, width=512, height=512, quality=50.0):
     return G
 
 
-def random_genome(rng, nxforms, final=False, variations=CONFIG1_VARIATIONS, coef_sigma=0.6):
+def random_genome(rng, nxforms, final=False, variations=VARIATIONS_0_19, coef_sigma=0.6):
     """Xforms with 2-4 variations drawn from `variations`, Dirichlet(1) weights,
     affine entries N(0, sigma^2), weights U(.2,1) normalised."""
     G = Genome(nxforms, final=final)
@@ -394,7 +394,7 @@ def random_genome(rng, nxforms, final=False, variations=CONFIG1_VARIATIONS, coef
     return G
 
 
-def config1_genome(seed=1, width=1920, height=1080, quality=2000.0, oversample=2, estimator=9.0):
+def still_genome(seed=1, width=1920, height=1080, quality=2000.0, oversample=2, estimator=9.0):
     """6 xforms + final, variations from 0-19, DE radius 9, gaussian r=1."""
     rng = np.random.default_rng(seed)
     G = random_genome(rng, 6, final=True)
@@ -403,7 +403,7 @@ def config1_genome(seed=1, width=1920, height=1080, quality=2000.0, oversample=2
     return G
 
 
-def config2_genomes(seed=2, width=1280, height=720, quality=500.0, temporal_samples=100, estimator=7.0):
+def animation_keys(seed=2, width=1280, height=720, quality=500.0, temporal_samples=100, estimator=7.0):
     """Two 5-xform genomes at times 0 and 120 for an interpolated animation."""
     rng = np.random.default_rng(seed)
     out = []
@@ -419,10 +419,10 @@ def config2_genomes(seed=2, width=1280, height=720, quality=500.0, temporal_samp
     return out
 
 
-CONFIG3_SIZES = [(256, 256), (512, 512), (1024, 768), (1920, 1080)]
+MIXED_SIZES = [(256, 256), (512, 512), (1024, 768), (1920, 1080)]
 
 
-def config3_jobs(seed=3, njobs=256, quality_scale=1.0):
+def mixed_jobs(seed=3, njobs=256, quality_scale=1.0):
     """Mixed-size batch: 2-12 xforms, size from 4 choices, quality
     log-uniform [50,1000], supersample 1|2, DE radius 0-11, bits 33 (90%)
     or 64 (10%).  Returns a list of (Genome, bits)."""
@@ -431,7 +431,7 @@ def config3_jobs(seed=3, njobs=256, quality_scale=1.0):
     for _ in range(njobs):
         nx = int(rng.integers(2, 13))
         G = random_genome(rng, nx)
-        w, h = CONFIG3_SIZES[int(rng.integers(0, 4))]
+        w, h = MIXED_SIZES[int(rng.integers(0, 4))]
         q = float(math.exp(rng.uniform(math.log(50), math.log(1000)))) * quality_scale
         ss = int(rng.integers(1, 3))
         est = float(rng.integers(0, 12))
@@ -442,11 +442,11 @@ def config3_jobs(seed=3, njobs=256, quality_scale=1.0):
     return jobs
 
 
-def config4_trace(seed=4, nrequests=64, rate_hz=4.0, quality_scale=1.0):
-    """Poisson arrivals: 95% config-3 style jobs, 5% 3840x2160 q1000 ss2 DE 11.
+def serving_trace(seed=4, nrequests=64, rate_hz=4.0, quality_scale=1.0):
+    """Poisson arrivals: 95% mixed-size jobs (as mixed_jobs), 5% 3840x2160 q1000 ss2 DE 11.
     Returns a list of (arrival_s, Genome, bits)."""
     rng = np.random.default_rng(seed)
-    small = config3_jobs(seed=seed + 100, njobs=nrequests, quality_scale=quality_scale)
+    small = mixed_jobs(seed=seed + 100, njobs=nrequests, quality_scale=quality_scale)
     t = 0.0
     out = []
     for i in range(nrequests):

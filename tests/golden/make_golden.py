@@ -121,9 +121,9 @@ RENDER_SETTINGS = [
 
 def render_genome(seed):
     if seed >= 5:
-        G = gm.config1_genome(seed, width=96, height=72, quality=30.0, oversample=1, estimator=4.0)
+        G = gm.still_genome(seed, width=96, height=72, quality=30.0, oversample=1, estimator=4.0)
     else:
-        G = gm.config0_genome(seed)
+        G = gm.small_genome(seed)
         gm.resize(G, 96, 72)
         G.g.sample_density = 30.0
     return G
@@ -148,7 +148,7 @@ ANIM_SETTINGS = [
 
 def make_anim_frame(setting):
     name, seed, bits, est, t, nts, nb = setting
-    gs = gm.config2_genomes(seed, width=96, height=72, quality=20.0, temporal_samples=nts, estimator=est)
+    gs = gm.animation_keys(seed, width=96, height=72, quality=20.0, temporal_samples=nts, estimator=est)
     for G in gs:
         G.g.nbatches = nb
     return gm.Frame(gs, bits=bits, nthreads=1, seed="golden-%s" % name, time=t)
@@ -266,7 +266,7 @@ def main():
             fil[key] = np.array([tf[i] for i in range(n)] + [td[i] for i in range(n)] + [s])
         for knum in range(14):
             for (ss, rad, field, aspect) in [(1, 0.5, 0, 1.0), (2, 1.0, 0, 1.0), (3, 0.7, 1, 1.3)]:
-                G = gm.config0_genome(0)
+                G = gm.small_genome(0)
                 G.g.spatial_filter_select = knum
                 G.g.spatial_oversample = ss
                 G.g.spatial_filter_radius = rad

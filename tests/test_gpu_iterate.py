@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 
 def test_chains_fp64_track_oracle(gpulib):
-    G = gm.config0_genome(3)
+    G = gm.small_genome(3)
     rng = np.random.default_rng(1)
     starts = np.stack([rng.uniform(-1, 1, 256), rng.uniform(-1, 1, 256), rng.uniform(0, 1, 256),
                        rng.uniform(0, 1, 256)], 1)
@@ -48,7 +48,7 @@ def test_chains_with_final_xform_and_xaos(gpulib):
 
 @pytest.mark.parametrize("palette_mode", [0, 1])
 def test_accumulate_matches_oracle(gpulib, palette_mode):
-    G = gm.config0_genome(1)
+    G = gm.small_genome(1)
     gm.resize(G, 64, 48)
     G.g.palette_mode = palette_mode
     G.g.rotate = 17.0 if palette_mode else 0.0
@@ -69,7 +69,7 @@ def test_accumulate_concentrated_points_match_oracle(gpulib):
     """Most points of a warp land in a handful of buckets: the warp-aggregated
     sums (shuffle reductions, one atomic per bucket) equal the oracle's
     one-by-one adds to FP32 rounding."""
-    G = gm.config0_genome(2)
+    G = gm.small_genome(2)
     gm.resize(G, 32, 24)
     F = gm.Frame(G)
     rng = np.random.default_rng(5)
@@ -104,7 +104,7 @@ def test_bounding_box_matches_oracle_chains(gpulib):
     from flam3_gb300 import abi as _abi
     from flam3_gb300.isaac import init_rc
 
-    G = gm.config1_genome(1, width=320, height=180, quality=10.0)
+    G = gm.still_genome(1, width=320, height=180, quality=10.0)
     nsamples, per = 200 * 1024, 1024
     rc = _abi.randctx()
     init_rc(rc, b"bb")
@@ -125,7 +125,7 @@ def test_colorhist_matches_oracle_chains(gpulib):
     from flam3_gb300 import abi as _abi
     from flam3_gb300.isaac import init_rc
 
-    G = gm.config1_genome(2, width=320, height=180, quality=10.0)
+    G = gm.still_genome(2, width=320, height=180, quality=10.0)
     rc = _abi.randctx()
     init_rc(rc, b"ch")
     h = render.colorhist(G, 20, rc)

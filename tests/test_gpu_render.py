@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 
 def cfg0(seed=0, w=256, h=192, q=50.0, bits=33, est=0.0):
-    G = gm.config0_genome(seed)
+    G = gm.small_genome(seed)
     gm.resize(G, w, h)
     G.g.sample_density = q
     G.g.estimator = est
@@ -119,7 +119,7 @@ def test_bits64_render_close_to_bits33(gpulib):
 
 
 def anim_frame(t, nts, est, q=400.0, bits=33, nthreads=8, rc_seed="anim", w=160, h=120):
-    gs = gm.config2_genomes(2, width=w, height=h, quality=q, temporal_samples=nts, estimator=est)
+    gs = gm.animation_keys(2, width=w, height=h, quality=q, temporal_samples=nts, estimator=est)
     return gm.Frame(gs, bits=bits, nthreads=nthreads, seed=rc_seed, time=t)
 
 
@@ -136,7 +136,7 @@ def test_animation_render_close_to_oracle(gpulib, t, nts, est, bits):
 
 
 def test_calc_nstrips_against_budget(gpulib):
-    F = gm.Frame(gm.config0_genome(3), bits=33, seed="ns")
+    F = gm.Frame(gm.small_genome(3), bits=33, seed="ns")
     need = render.memory_required(F)
     assert render.calc_nstrips(F, need * 10) == 1
     assert render.calc_nstrips(F, need / 2.5) == 3
@@ -147,7 +147,7 @@ def test_render_strips_matches_full_render(gpulib):
     """flam3-render's strip loop: one strip is the plain render; three strips
     (the last one shorter) carry the same image up to sampling noise, and the
     caller's genome is unchanged."""
-    G = gm.config0_genome(4, width=200, height=250, quality=200.0)
+    G = gm.small_genome(4, width=200, height=250, quality=200.0)
     F = gm.Frame(G, bits=33, seed="strips")
     full, st_full = render.render(F)
     F1 = gm.Frame(G, bits=33, seed="strips")

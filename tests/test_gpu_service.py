@@ -28,21 +28,21 @@ def frame(kind, seed=0):
     """Small frames covering the tail shapes: fused log, fused DE, several
     batches, temporal samples, FP64 buckets, fields, earlyclip, RGBA16."""
     if kind == "plain":
-        G = gm.config0_genome(seed)
+        G = gm.small_genome(seed)
         gm.resize(G, 200, 150)
         G.g.sample_density = 40.0
         return gm.Frame(G, bits=33, seed="svc-%s-%d" % (kind, seed))
     if kind == "de":
-        G = gm.config0_genome(seed)
+        G = gm.small_genome(seed)
         gm.resize(G, 160, 120)
         G.g.sample_density = 60.0
         G.g.estimator = 4.0
         return gm.Frame(G, bits=33, seed="svc-%s-%d" % (kind, seed))
     if kind == "b64_ss2_de":
-        G = gm.config1_genome(seed + 5, width=128, height=96, quality=30.0, oversample=2, estimator=5.0)
+        G = gm.still_genome(seed + 5, width=128, height=96, quality=30.0, oversample=2, estimator=5.0)
         return gm.Frame(G, bits=64, seed="svc-%s-%d" % (kind, seed))
     if kind == "batches":
-        G = gm.config0_genome(seed)
+        G = gm.small_genome(seed)
         gm.resize(G, 120, 90)
         G.g.sample_density = 40.0
         G.g.nbatches = 3
@@ -50,15 +50,15 @@ def frame(kind, seed=0):
         G.g.estimator = 3.0
         return gm.Frame(G, bits=33, seed="svc-%s-%d" % (kind, seed))
     if kind == "anim":
-        gs = gm.config2_genomes(seed + 2, width=144, height=96, quality=40.0, temporal_samples=6, estimator=3.0)
+        gs = gm.animation_keys(seed + 2, width=144, height=96, quality=40.0, temporal_samples=6, estimator=3.0)
         return gm.Frame(gs, bits=33, seed="svc-%s-%d" % (kind, seed), time=30.0 + seed)
     if kind == "early":
-        G = gm.config0_genome(seed)
+        G = gm.small_genome(seed)
         gm.resize(G, 100, 80)
         G.g.sample_density = 30.0
         return gm.Frame(G, bits=64, seed="svc-%s-%d" % (kind, seed), earlyclip=1)
     if kind == "rgba16":
-        G = gm.config0_genome(seed)
+        G = gm.small_genome(seed)
         gm.resize(G, 96, 64)
         G.g.sample_density = 30.0
         return gm.Frame(G, bits=33, seed="svc-%s-%d" % (kind, seed), bytes_per_channel=2)

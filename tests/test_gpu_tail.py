@@ -30,7 +30,7 @@ CASES = [
 
 
 def frame(seed, bits, est, ss, early, bpc, filt, w=120, h=90, q=40.0):
-    G = gm.config0_genome(seed)
+    G = gm.small_genome(seed)
     gm.resize(G, w, h)
     G.g.sample_density = q
     G.g.estimator = est

@@ -71,7 +71,7 @@ def test_strip_planning_without_gpu():
     checks are host logic (flam3-render.c:35-101, 276-283)"""
     from flam3_gb300 import genome as gm, render
 
-    F = gm.Frame(gm.config0_genome(3, width=64, height=40), bits=33, seed="s")
+    F = gm.Frame(gm.small_genome(3, width=64, height=40), bits=33, seed="s")
     need = render.memory_required(F)
     assert need > 0
     assert render.calc_nstrips(F, need) == 1
@@ -86,7 +86,7 @@ def test_analysis_helpers_need_a_random_context():
     from flam3_gb300 import genome as gm, render
 
     lib = render.load()
-    G = gm.config0_genome(3)
+    G = gm.small_genome(3)
     assert lib.flam3gpu_dimension(C.byref(G.g), 1000, 0, None) == -1.0
     assert b"ISAAC" in lib.flam3gpu_last_error()
     assert lib.flam3gpu_lyapunov(C.byref(G.g), 10, None) == -1.0

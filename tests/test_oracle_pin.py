@@ -80,7 +80,7 @@ def test_oracle_filters_match_reference():
         assert rel_close([tf[i] for i in range(n)] + [td[i] for i in range(n)] + [s], d[key])
     for key in [k for k in d.files if k.startswith("sf_")]:
         _, knum, ss, rad, field, aspect = key.split("_")
-        G = gm.config0_genome(0)
+        G = gm.small_genome(0)
         G.g.spatial_filter_select = int(knum)
         G.g.spatial_oversample = int(ss)
         G.g.spatial_filter_radius = float(rad)
@@ -112,7 +112,7 @@ def test_oracle_renders_match_reference_directly(seed, bits, nt, est):
     ref = _oracle.reference(True)
     outs = []
     for which in ("ref", "oracle"):
-        G = gm.config0_genome(seed)
+        G = gm.small_genome(seed)
         gm.resize(G, 80, 60)
         G.g.sample_density = 20.0
         G.g.estimator = est

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _frame(seed, est, bits=33, w=160, h=120, q=60.0):
-    G = gm.config0_genome(seed)
+    G = gm.small_genome(seed)
     gm.resize(G, w, h)
     G.g.sample_density = q
     G.g.estimator = est
