@@ -232,7 +232,7 @@ out:
 
 int f3g_pack_genome(flam3_genome *cp, F3GPass *pass) {
   if (cp->num_xforms > F3G_MAX_XFORMS) {
-    f3g_set_error("genome has %d xforms; this build handles up to %d", cp->num_xforms, F3G_MAX_XFORMS);
+    f3g_set_error("genome has %d xforms; the library handles up to %d", cp->num_xforms, F3G_MAX_XFORMS);
     return 1;
   }
   static const size_t prm_off[PRM_COUNT] = {

@@ -746,7 +746,7 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
     if (de_on) {
       int R = (int)ceil(de_w[0]) - 1;
       if (R > f3g_de_max_reach()) {
-        f3g_set_error("density estimation radius %d exceeds this build's limit %d", R, f3g_de_max_reach());
+        f3g_set_error("density estimation radius %d exceeds the library's limit %d", R, f3g_de_max_reach());
         goto done;
       }
       int nk = mfi + 1;

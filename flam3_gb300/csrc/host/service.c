@@ -376,7 +376,7 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
     if (b->de_on) {
       b->R = (int)ceil(de_w[0]) - 1;
       if (b->R > f3g_de_max_reach()) {
-        f3g_set_error("density estimation radius %d exceeds this build's limit %d", b->R, f3g_de_max_reach());
+        f3g_set_error("density estimation radius %d exceeds the library's limit %d", b->R, f3g_de_max_reach());
         goto done;
       }
       b->nk = mfi + 1;
