@@ -65,3 +65,35 @@ def test_tail_matches_oracle_on_same_histogram(gpulib, case):
     frac_ok = float(np.mean(d <= 1))
     assert frac_ok >= 0.999, (frac_ok, int(d.max()))
     assert ref.mean() > 1.0
+
+
+# every filter width the separable strip kernel is instantiated for
+# (oversample 1: 1, 3, 5, 7; oversample 2: 2, 4, 8, 10, 14, 16), with and
+# without earlyclip, FP32 and FP64 histograms
+STRIP_CASES = [
+    # id, ss, gaussian radius, bits, earlyclip, filter width (filters.c:217-270)
+    ("ss1_r0.3", 1, 0.3, 33, 0, 1), ("ss1_r0.5_b64", 1, 0.5, 64, 0, 3), ("ss1_r1_early", 1, 1.0, 33, 1, 5),
+    ("ss1_r2_b64_early", 1, 2.0, 64, 1, 7),
+    ("ss2_r0.3", 2, 0.3, 33, 0, 2), ("ss2_r0.5_early", 2, 0.5, 33, 1, 4), ("ss2_r1_b64", 2, 1.0, 64, 0, 8),
+    ("ss2_r1.5", 2, 1.5, 33, 0, 10), ("ss2_r2_b64_early", 2, 2.0, 64, 1, 14), ("ss2_r2.5", 2, 2.5, 33, 0, 16),
+]
+
+
+@pytest.mark.parametrize("case", STRIP_CASES, ids=[c[0] for c in STRIP_CASES])
+def test_strip_tail_widths_match_oracle(gpulib, case):
+    cid, ss, radius, bits, early, fw_expect = case
+
+    def mk():
+        F = frame(5, bits, 0.0, ss, early, 1, 0, w=150, h=110)
+        F.genomes[0].g.spatial_filter_radius = radius
+        F.sync()
+        return F
+
+    F = mk()
+    ref, st, ex = _oracle.oracle_render(F, want_hist=True)
+    fw = render.histogram_dims(mk())["filter_width"]
+    assert fw == fw_expect
+    out, _, _ = render.render(mk(), hist_in=ex["hist"])
+    d = np.abs(out.astype(np.int64) - ref.astype(np.int64))
+    assert float(np.mean(d <= 1)) >= 0.999, (cid, fw, float(np.mean(d <= 1)), int(d.max()))
+    assert ref.mean() > 1.0
