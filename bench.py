@@ -342,11 +342,14 @@ def mae(a, b):
     return float(np.mean(np.abs(a.astype(np.float64) - b.astype(np.float64))))
 
 
-def leg_batched(name, make_frames, note):
-    """plain drop-in one frame at a time vs one flam3gpu_render_batch call"""
+def leg_batched(name, make_frames, note, warm=8):
+    """plain drop-in one frame at a time vs one batch on a render service;
+    both arms warmed first on `warm` frames (allocations, pools, graphs)"""
     import torch
     from flam3_gb300 import render, service
 
+    for F in make_frames("w")[:warm]:
+        render.render(F)
     frames = make_frames("p")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -361,22 +364,27 @@ def leg_batched(name, make_frames, note):
             dev[k] += t[k]
     t_plain = time.perf_counter() - t0
     frames = make_frames("p")  # same seeds: same samples, up to atomic order
+    keys = ("rounds", "launches", "tail_graphs", "graphs_instantiated", "host_admit_s", "host_round_s",
+            "host_tail_s", "host_complete_s", "host_wait_s", "gpu_iterate_s", "gpu_tail_s")
     with service.Service(round_samples=-1) as svc:  # one persistent launch per round over all frames
+        for t in svc.submit_many(make_frames("w")[:warm]):
+            svc.wait(t)
+        c0 = svc.counters()
         t0 = time.perf_counter()
         tk = svc.submit_many(frames)
         res = [svc.wait(t)[:2] for t in tk]
         t_batch = time.perf_counter() - t0
-        cnt = svc.counters()
+        c1 = svc.counters()
+    cnt = {k: c1[k] - c0[k] for k in keys}
+    cnt["peak_device_bytes"] = c1["peak_device_bytes"]
     n = len(frames)
     diff = max(mae(a, b[0]) for a, b in zip(plain_imgs, res))
-    return {"workload": note, "renders": n, "iterations": iters,
+    return {"workload": note, "renders": n, "iterations": iters, "warmup_renders_per_arm": warm,
             "plain_renders_per_s": n / t_plain, "batched_renders_per_s": n / t_batch,
             "speedup": t_plain / t_batch, "plain_s": t_plain, "batched_s": t_batch,
             "plain_giter_s": iters / t_plain / 1e9, "batched_giter_s": iters / t_batch / 1e9,
             "plain_device_s": {k.replace("_ms", "_s"): v / 1e3 for k, v in dev.items()},
-            "max_mae_batched_vs_plain": diff, "service": {k: cnt[k] for k in (
-                "rounds", "launches", "tail_graphs", "graphs_instantiated", "peak_device_bytes", "host_admit_s",
-                "host_round_s", "host_tail_s", "host_complete_s", "host_wait_s", "gpu_iterate_s", "gpu_tail_s")}}
+            "max_mae_batched_vs_plain": diff, "service": cnt}
 
 
 def leg_served(nreq, seed=4, ref_check=3):
@@ -388,7 +396,19 @@ def leg_served(nreq, seed=4, ref_check=3):
         tr = gm.serving_trace(seed=seed, nrequests=nreq, rate_hz=rate)
         return [(t, gm.Frame(G, bits=b, seed="srv-%d" % i)) for i, (t, G, b) in enumerate(tr)]
 
+    def warm_up(svc=None, n=8):
+        """a few requests of another trace, so both arms start warm"""
+        wr = gm.serving_trace(seed=seed + 1000, nrequests=n, rate_hz=1.0)
+        fr = [gm.Frame(G, bits=b, seed="warm-%d" % i) for i, (_, G, b) in enumerate(wr)]
+        if svc is None:
+            for F in fr:
+                render.render(F)
+        else:
+            for t in [svc.submit(F) for F in fr]:
+                svc.wait(t)
+
     # saturation: every request queued at t=0
+    warm_up()
     reqs = trace(1.0)
     t0 = time.perf_counter()
     plain_imgs = []
@@ -400,12 +420,18 @@ def leg_served(nreq, seed=4, ref_check=3):
             dev[k] += t[k]
     t_plain = time.perf_counter() - t0
     reqs = trace(1.0)
+    keys = ("rounds", "launches", "tail_graphs", "graphs_instantiated", "host_admit_s", "host_round_s",
+            "host_tail_s", "host_complete_s", "host_wait_s", "gpu_iterate_s", "gpu_tail_s")
     with service.Service() as svc:
+        warm_up(svc)
+        c0 = svc.counters()
         t0 = time.perf_counter()
         tk = [svc.submit(F) for _, F in reqs]
         served_imgs = [svc.wait(t)[0] for t in tk]
         t_served = time.perf_counter() - t0
-        cnt = svc.counters()
+        c1 = svc.counters()
+    cnt = {k: c1[k] - c0[k] for k in keys}
+    cnt["peak_device_bytes"] = c1["peak_device_bytes"]
     cap_plain = nreq / t_plain
     # latency at 70% of the plain path's capacity (a load the plain path sustains)
     rate = 0.7 * cap_plain
@@ -421,6 +447,7 @@ def leg_served(nreq, seed=4, ref_check=3):
     reqs = trace(rate)
     lat_served = []
     with service.Service() as svc:
+        warm_up(svc)
         tickets = []
         start = time.perf_counter()
         for t_arr, F in reqs:
@@ -449,9 +476,7 @@ def leg_served(nreq, seed=4, ref_check=3):
             "speedup": t_plain / t_served, "rate_hz": rate,
             "latency_ms_plain": q(lat_plain), "latency_ms_served": q(lat_served),
             "mean_mae_served_vs_plain": float(np.mean(diffs)), "max_mae_served_vs_plain": float(np.max(diffs)),
-            "error_vs_16x": errs, "service": {k: cnt[k] for k in (
-                "rounds", "launches", "tail_graphs", "graphs_instantiated", "peak_device_bytes", "host_admit_s",
-                "host_round_s", "host_tail_s", "host_complete_s", "host_wait_s", "gpu_iterate_s", "gpu_tail_s")}}
+            "error_vs_16x": errs, "warmup_requests_per_arm": 8, "service": cnt}
 
 
 def run_legs(args):
