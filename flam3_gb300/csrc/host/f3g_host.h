@@ -48,6 +48,12 @@ int f3g_camera(flam3_frame *spec, const flam3_genome *cp, int field, const f3g_g
 void f3g_pass_key(flam3_frame *spec, uint32_t key[2]);
 unsigned long f3g_irand(randctx *r);
 
+/* genome helpers (interp.c) for the XML genome reader (xml.c) */
+void f3g_clear_cp(flam3_genome *cp, int default_flag);
+void f3g_add_xforms(flam3_genome *cp, int num_to_add, int interp_padding, int final_flag);
+void f3g_rgb2hsv(const double *rgb, double *hsv);
+void f3g_hsv2rgb(const double *hsv, double *rgb);
+
 /* error reporting: message kept per thread, also printed to stderr */
 void f3g_set_error(const char *fmt, ...);
 void f3g_clear_error(void);

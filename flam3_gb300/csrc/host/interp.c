@@ -163,6 +163,8 @@ static void free_genome(flam3_genome *g) {
       for (int i = 0; i < ns; i++) free(g->chaos[i]);
       free(g->chaos);
     }
+    for (int i = 0; i < g->num_xforms; i++)
+      if (g->xform[i].num_motion > 0) free(g->xform[i].motion);
     free(g->xform);
   }
   g->xform = NULL;
@@ -770,3 +772,54 @@ int flam3gpu_interpolate(flam3_genome *cps, int ncps, double time, double stagge
 }
 
 void flam3gpu_free_genome(flam3_genome *g) { free_genome(g); }
+
+/* ---- helpers for the genome reader (xml.c) ---- */
+
+/* clear_cp (flam3.c:1270-1368): defaults (default_flag 1) or the
+ * "unset" markers (0), xforms, chaos and motion elements released */
+void f3g_clear_cp(flam3_genome *cp, int default_flag) {
+  free_genome(cp);
+  const double time = cp->time;
+  char name[flam3_name_len + 1];
+  memcpy(name, cp->flame_name, sizeof(name));
+  flam3_palette pal;
+  memcpy(pal, cp->palette, sizeof(pal));
+  void *edits = cp->edits;
+  const int chaos_enable = cp->chaos_enable;
+  clear_defaults(cp);
+  if (default_flag != 1) {
+    cp->highlight_power = -1.0;
+    cp->background[0] = cp->background[1] = cp->background[2] = -1.0;
+    cp->zoom = 999999999;
+    cp->spatial_oversample = -1;
+    cp->spatial_filter_radius = -1;
+    cp->width = -1;
+    cp->height = -1;
+    cp->sample_density = -1;
+    cp->estimator = -1;
+    cp->estimator_minimum = -1;
+    cp->estimator_curve = -1;
+    cp->gam_lin_thresh = -1;
+    cp->nbatches = 0;
+    cp->ntemporal_samples = 0;
+    cp->spatial_filter_select = -1;
+    cp->interpolation_type = -1;
+    cp->temporal_filter_type = -1;
+    cp->temporal_filter_width = -1;
+    cp->temporal_filter_exp = -999;
+    cp->palette_mode = -1;
+  }
+  /* fields clear_cp does not touch keep their values */
+  cp->time = time;
+  memcpy(cp->flame_name, name, sizeof(name));
+  memcpy(cp->palette, pal, sizeof(pal));
+  cp->edits = edits;
+  cp->chaos_enable = chaos_enable;
+}
+
+void f3g_add_xforms(flam3_genome *cp, int num_to_add, int interp_padding, int final_flag) {
+  add_xforms(cp, num_to_add, interp_padding, final_flag);
+}
+
+void f3g_rgb2hsv(const double *rgb, double *hsv) { rgb2hsv(rgb, hsv); }
+void f3g_hsv2rgb(const double *hsv, double *rgb) { hsv2rgb(hsv, rgb); }

@@ -177,6 +177,46 @@ class Frame:
 # seeded synthetic workloads
 # ---------------------------------------------------------------------------
 
+def genome_from_struct(src):
+    """A Genome holding a copy of a C flam3_genome (xforms, chaos rows;
+    motion elements and edits are not carried)."""
+    nx = src.num_xforms
+    final = src.final_xform_index >= 0
+    num_std = nx - (1 if final else 0)
+    G = Genome(num_std, final=final)
+    C.memmove(C.addressof(G.g), C.addressof(src), C.sizeof(abi.flam3_genome))
+    # the pointers back to this Genome's own storage
+    G.g.xform = C.cast(G._xforms, C.POINTER(abi.flam3_xform))
+    G.g.chaos = C.cast(G._chaos, C.POINTER(C.POINTER(C.c_double)))
+    G.g.edits = None
+    for i in range(nx):
+        C.memmove(C.addressof(G._xforms[i]), C.addressof(src.xform[i]), C.sizeof(abi.flam3_xform))
+        G._xforms[i].motion = None
+        G._xforms[i].num_motion = 0
+    for i in range(num_std):
+        for j in range(num_std):
+            G._chaos_rows[i][j] = src.chaos[i][j]
+    return G
+
+
+def parse_flam3(xml, filename="", default_flag=1):
+    """flam3_parse_xml2 through the library's reader: the <flame> elements of
+    an XML text (str or bytes) as Genomes."""
+    from . import render
+    lib = render.load()
+    data = xml.encode() if isinstance(xml, str) else bytes(xml)
+    n = C.c_int(0)
+    p = lib.flam3gpu_parse_xml2(C.c_char_p(data), C.c_char_p(filename.encode()), default_flag, C.byref(n))
+    if not p:
+        raise render.Flam3GpuError("flam3gpu_parse_xml2 failed: " + lib.flam3gpu_last_error().decode())
+    try:
+        return [genome_from_struct(p[i]) for i in range(n.value)]
+    finally:
+        for i in range(n.value):
+            lib.flam3gpu_free_genome(C.byref(p[i]))
+        C.CDLL(None).free(C.cast(p, C.c_void_p))
+
+
 def random_palette(rng, ncontrol=8):
     """256-entry RGB gradient through `ncontrol` U(0,1) control colours."""
     ctl = rng.uniform(0.0, 1.0, size=(ncontrol, 3))

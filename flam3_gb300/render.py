@@ -73,6 +73,8 @@ def load():
     lib.flam3gpu_dimension.restype = C.c_double
     lib.flam3gpu_lyapunov.argtypes = [G, C.c_int, C.POINTER(abi.randctx)]
     lib.flam3gpu_lyapunov.restype = C.c_double
+    lib.flam3gpu_parse_xml2.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int)]
+    lib.flam3gpu_parse_xml2.restype = C.POINTER(abi.flam3_genome)
     lib.flam3gpu_free_genome.argtypes = [G]
     lib.flam3gpu_free_genome.restype = None
     lib.flam3gpu_set_interpolator.argtypes = [C.c_void_p]

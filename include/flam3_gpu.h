@@ -216,6 +216,19 @@ int flam3gpu_render(flam3_frame *f, void *out, int field, int nchan, int transp,
  * render of f->genomes[0] needs (histogram + accumulator + chain state). */
 double flam3gpu_render_memory_required(flam3_frame *f);
 
+/* Replaces flam3_parse_xml2 (flam3.h:581, flam3.c:1423-1485, parser.c): reads
+ * flam3's XML genome format (every <flame> element, at any depth, in
+ * document order) into a malloc'd array of *ncps genomes with the
+ * reference's defaults (default_flag 1) or unset markers (0), palettes
+ * (inline <color>/<colors>/<palette> data, missing entries interpolated,
+ * library palettes by number from the file named by $flam3_palettes),
+ * <symmetry>, xforms, final xform, motion elements, xaos and solo xform.
+ * xmlfilename's base name goes to parent_fname.  Free each genome with
+ * flam3gpu_free_genome, then the array with free().  Returns NULL (and
+ * *ncps = 0) on malformed XML or a malformed flame.  <edit> elements are not
+ * kept (edits stays NULL). */
+flam3_genome *flam3gpu_parse_xml2(char *xmldata, char *xmlfilename, int default_flag, int *ncps);
+
 /* Replaces calc_nstrips (flam3-render.c:35-101) for device memory: the number
  * of horizontal strips the still f needs so that each strip's device bytes
  * (flam3gpu_render_memory_required) fit budget_bytes, or 80 % of the free

@@ -170,3 +170,23 @@ def test_render_strips_matches_full_render(gpulib):
         assert three[r0 + 1:r0 + 82].mean() > 0.5 * full[r0:r0 + 81].mean()
     with pytest.raises(render.Flam3GpuError):
         render.render_strips(gm.Frame(G, bits=33, seed="x"), 251)
+
+
+FLAME_XML = """<flames><flame name="xml test" size="160 120" center="0 0" scale="40" quality="400"
+  oversample="1" filter="0.5" estimator_radius="4" brightness="4" gamma="4">
+  <xform weight="0.4" color="0" linear="0.6" spherical="0.4" coefs="0.5 0.3 -0.3 0.5 0.4 0.1"/>
+  <xform weight="0.3" color="0.5" sinusoidal="1" coefs="0.6 0 0 0.6 -0.4 0.2"/>
+  <xform weight="0.3" color="1" julia="0.7" swirl="0.3" coefs="0.4 -0.2 0.2 0.4 0 -0.5"/>
+  <finalxform color="0.5" color_speed="0" linear="0.8" polar="0.2" coefs="1 0 0 1 0 0"/>
+  <color index="0" rgb="255 40 0"/><color index="128" rgb="40 255 80"/><color index="255" rgb="20 60 255"/>
+</flame></flames>"""
+
+
+def test_render_of_parsed_genome_close_to_oracle(gpulib):
+    """a genome read from flam3's XML format renders on the GPU like the
+    oracle renders the same genome"""
+    G = gm.parse_flam3(FLAME_XML, "test.flam3")[0]
+    o, _, _ = _oracle.oracle_render(gm.Frame(G, bits=33, nthreads=8, seed="xml"))
+    g, _ = render.render(gm.Frame(G, bits=33, seed="xml-g"))
+    assert o.mean() > 5.0
+    assert mae(o, g) < 2.5
