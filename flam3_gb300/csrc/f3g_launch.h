@@ -89,6 +89,14 @@ int f3g_launch_iterate_chains(const F3GPass *d_pass, int nchains, int n, int fus
                               uint32_t key0, uint32_t key1, double *d_samples, unsigned long long *d_bad,
                               int precision, cudaStream_t st);
 
+/* PNG encoder (f3g_png.cu) */
+long long f3g_png_filtered_bytes(int w, int h, int nchan, int bpc);
+int f3g_png_segments(int w, int h, int nchan, int bpc);
+size_t f3g_png_work_bytes(int w, int h, int nchan, int bpc);
+size_t f3g_png_idat_bound(int w, int h, int nchan, int bpc);
+int f3g_png_encode_idat(const void *d_img, int w, int h, int nchan, int bpc, void *d_work, void *d_idat,
+                        unsigned long long *d_len, cudaStream_t st);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,11 @@ typedef struct {
   float *d_de_w; size_t de_w_bytes;
   float *d_de_c; size_t de_c_bytes;
   double timings[8];
+  /* PNG encoder (png.c): scratch, IDAT chunks, their length, host images */
+  void *d_png_work; size_t png_work_bytes;
+  void *d_png_idat; size_t png_idat_bytes;
+  void *d_png_img; size_t png_img_bytes;
+  unsigned long long *d_png_len, *h_png_len; /* pinned */
 } f3g_ctx;
 
 f3g_ctx *f3g_get_ctx(void);

@@ -504,6 +504,12 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
   if (io) {
     io->hist_w = g.W;
     io->hist_h = g.H;
+    io->image_w = g.image_width;
+    io->image_h = g.image_height;
+  }
+  if (!out && !(io && io->keep_on_device)) {
+    f3g_set_error("no output buffer");
+    goto done;
   }
   double sumfilt = f3g_temporal_filter(nbatches * ntemporal, cp.temporal_filter_type, cp.temporal_filter_exp,
                                        cp.temporal_filter_width, &tfilter, &tdeltas);
@@ -871,6 +877,22 @@ tail_fused:;
       goto done;
     }
     CK(cudaEventRecord(c->ev[5], c->stream));
+    if (io && io->keep_on_device) {
+      /* the image stays in c->d_out for the caller's next device step */
+      float ms = 0;
+      CK(cudaEventSynchronize(c->ev[5]));
+      cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]);
+      t_tail = ms;
+      if (pending_ctr) {
+        float mi = 0;
+        cudaEventElapsedTime(&mi, c->ev[0], c->ev[1]);
+        t_iter += mi;
+        stats->badvals += (double)c->h_ctr->badvals;
+        plotted += (double)c->h_ctr->plotted;
+      }
+      rv = 0;
+      goto done;
+    }
     size_t row = (size_t)g.image_width * nchan * spec->bytes_per_channel;
     unsigned char *dst = (unsigned char *)out;
     if (field == flam3_field_odd) dst += row;

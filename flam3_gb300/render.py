@@ -25,13 +25,22 @@ class Flam3GpuError(RuntimeError):
 class RenderIO(C.Structure):
     _fields_ = [("hist_in", C.POINTER(C.c_double)), ("hist_out", C.POINTER(C.c_double)),
                 ("accum_out", C.POINTER(C.c_double)), ("hist_w", C.c_int), ("hist_h", C.c_int),
-                ("reserved", C.c_int * 6)]
+                ("keep_on_device", C.c_int), ("image_w", C.c_int), ("image_h", C.c_int),
+                ("reserved", C.c_int * 3)]
 
 
 class Options(C.Structure):
     _fields_ = [("iter_mode", C.c_int), ("iter_precision", C.c_int), ("shuffle_every", C.c_int),
                 ("threads_per_block", C.c_int), ("blocks", C.c_int), ("chain_samples", C.c_int),
                 ("seed_salt", C.c_uint64), ("de_tile", C.c_int), ("reserved", C.c_int * 7)]
+
+
+class PngText(C.Structure):
+    _fields_ = [("key", C.c_char_p), ("text", C.c_char_p), ("compressed", C.c_int)]
+
+
+class ImgComments(C.Structure):
+    _fields_ = [("genome", C.c_char_p), ("badvals", C.c_char_p), ("numiters", C.c_char_p), ("rtime", C.c_char_p)]
 
 
 def load():
@@ -79,6 +88,12 @@ def load():
     lib.flam3gpu_free_genome.restype = None
     lib.flam3gpu_set_interpolator.argtypes = [C.c_void_p]
     lib.flam3gpu_set_interpolator.restype = None
+    ucpp = C.POINTER(C.POINTER(C.c_ubyte))
+    lib.flam3gpu_encode_png.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.POINTER(PngText), C.c_int, ucpp, C.POINTER(C.c_size_t)]
+    lib.flam3gpu_write_png.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(ImgComments), C.c_int]
+    lib.flam3gpu_render_png.argtypes = [F, C.c_int, S, C.c_char_p, ucpp, C.POINTER(C.c_size_t)]
+    lib.flam3gpu_png_last_ms.argtypes = [dp]
     _LIB = lib
     return lib
 
@@ -317,3 +332,87 @@ def colorhist(genome, num_batches=10, rc=None):
         _err(lib, "flam3gpu_colorhist")
     return hist
 
+
+
+_libc = None
+
+
+def _take_buffer(ptr, n):
+    """Copies a malloc'd buffer of the library into bytes and frees it."""
+    global _libc
+    if _libc is None:
+        _libc = C.CDLL(None)
+        _libc.free.argtypes = [C.c_void_p]
+    data = C.string_at(ptr, n)
+    _libc.free(C.cast(ptr, C.c_void_p))
+    return data
+
+
+def encode_png(image, texts=(), on_device_ptr=None):
+    """PNG bytes of an (h, w, 3|4) uint8 or uint16 image, encoded on the GPU
+    (flam3gpu_encode_png).  texts: (key, text, compressed) tuples.  With
+    on_device_ptr the pixels are read from that device address instead (the
+    array then only gives shape and dtype)."""
+    lib = load()
+    img = np.ascontiguousarray(image)
+    if img.ndim != 3 or img.shape[2] not in (3, 4) or img.dtype not in (np.uint8, np.uint16):
+        raise ValueError("image must be (h, w, 3|4) uint8 or uint16")
+    h, w, nchan = img.shape
+    bpc = img.dtype.itemsize
+    tt = (PngText * max(1, len(texts)))()
+    keep = []
+    for i, (k, t, z) in enumerate(texts):
+        kb = k.encode("latin-1")
+        tb = None if t is None else t.encode("latin-1")
+        keep += [kb, tb]
+        tt[i] = PngText(kb, tb, int(z))
+    out = C.POINTER(C.c_ubyte)()
+    n = C.c_size_t()
+    src = on_device_ptr if on_device_ptr is not None else img.ctypes.data
+    if lib.flam3gpu_encode_png(C.c_void_p(src), int(on_device_ptr is not None), w, h, nchan, bpc, tt, len(texts),
+                               C.byref(out), C.byref(n)):
+        _err(lib, "flam3gpu_encode_png")
+    return _take_buffer(out, n.value)
+
+
+def write_png(path, image, genome=None, badvals=None, numiters=None, rtime=None):
+    """write_png (png.c:36) on the GPU: an (h, w, 4) uint8/uint16 image to `path`."""
+    lib = load()
+    img = np.ascontiguousarray(image)
+    if img.ndim != 3 or img.shape[2] != 4 or img.dtype not in (np.uint8, np.uint16):
+        raise ValueError("image must be (h, w, 4) uint8 or uint16")
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    libc.fclose.argtypes = [C.c_void_p]
+    enc = (lambda v: None if v is None else v.encode("latin-1"))
+    fpc = ImgComments(enc(genome), enc(badvals), enc(numiters), enc(rtime))
+    fp = libc.fopen(path.encode(), b"wb")
+    if not fp:
+        raise OSError(f"cannot open {path}")
+    try:
+        rv = lib.flam3gpu_write_png(fp, img.ctypes.data, img.shape[1], img.shape[0], C.byref(fpc), img.dtype.itemsize)
+    finally:
+        libc.fclose(fp)
+    if rv:
+        _err(lib, "flam3gpu_write_png")
+
+
+def render_png(frame, transp=0, genome_xml=None):
+    """flam3gpu_render_png: (png bytes, stats) of an RGBA render that never
+    leaves the device as raw pixels."""
+    lib = load()
+    st = abi.stat_struct()
+    out = C.POINTER(C.c_ubyte)()
+    n = C.c_size_t()
+    if lib.flam3gpu_render_png(C.byref(frame.f), transp, C.byref(st),
+                               None if genome_xml is None else genome_xml.encode("latin-1"), C.byref(out), C.byref(n)):
+        _err(lib, "flam3gpu_render_png")
+    return _take_buffer(out, n.value), st
+
+
+def png_last_ms():
+    """Kernel time (ms) of this thread's last PNG encode."""
+    v = C.c_double()
+    load().flam3gpu_png_last_ms(C.byref(v))
+    return v.value

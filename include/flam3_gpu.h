@@ -26,6 +26,7 @@
 
 #include <stddef.h>
 #include <stdint.h>
+#include <stdio.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -249,6 +250,57 @@ int flam3gpu_calc_nstrips(flam3_frame *f, double budget_bytes);
  * the whole frame's samples, so nstrips times the plain render's).
  * Returns 0 on success, 1 on failure (also when nstrips exceeds the height). */
 int flam3gpu_render_strips(flam3_frame *f, void *out, int nchan, int transp, stat_struct *stats, int nstrips);
+
+/* ---- PNG output on the device ---- */
+
+/* Comments write_png stores in the PNG (img.h:29-36, the same layout). */
+typedef struct {
+  char *genome;
+  char *badvals;
+  char *numiters;
+  char *rtime;
+} flam3gpu_img_comments;
+
+/* One PNG text chunk: tEXt, or zTXt when `compressed` (NULL or empty text:
+ * an empty tEXt chunk, as libpng writes it). */
+typedef struct {
+  const char *key;
+  const char *text;
+  int compressed;
+} flam3gpu_png_text;
+
+/* Encodes a packed image as a PNG in host memory (the pixel path of
+ * write_png, png.c:36-116: per-row PNG filters chosen by the
+ * minimum-sum-of-absolute-values rule, deflate, IDAT chunks) with the
+ * filtering, deflate, CRC-32 and Adler-32 done on the device.  image is
+ * width x height pixels of nchan (3: RGB, 4: RGBA) samples of bpc bytes
+ * (16-bit samples in host byte order, as flam3_render writes them), in
+ * device memory when image_on_device, else in host memory.  The text chunks
+ * follow IHDR in the given order.  *png receives a malloc'd buffer (release
+ * it with free) and *png_len its size.  Returns 0, or 1 on failure. */
+int flam3gpu_encode_png(const void *image, int image_on_device, int width, int height, int nchan, int bpc,
+                        const flam3gpu_png_text *text, int ntext, unsigned char **png, size_t *png_len);
+
+/* Replaces write_png (png.c:36, img.h:40): writes the RGBA image (bpc 1 or
+ * 2) to `file` as a PNG with write_png's text chunks (flam3_version,
+ * flam3_nickname/url/id from $nick/$url/$id, flam3_error_rate,
+ * flam3_samples, flam3_time, and the genome as zTXt; none when
+ * $enable_png_comments is not 1).  Returns 0, or 1 after a message on
+ * stderr (the reference returns nothing and prints through perror). */
+int flam3gpu_write_png(FILE *file, void *image, int width, int height, flam3gpu_img_comments *fpc, int bpc);
+
+/* flam3-render's render-and-write step (flam3-render.c:345-378) without
+ * the image leaving the device: renders f as flam3gpu_render(f, out,
+ * flam3_field_both, 4, transp, stats) does, then encodes the RGBA image on
+ * the device with the comments flam3-render passes to write_png (error rate,
+ * samples and seconds from stats; genome_xml, may be NULL, as the genome).
+ * *png receives a malloc'd PNG (release it with free).  Returns 0, or 1 on
+ * failure. */
+int flam3gpu_render_png(flam3_frame *f, int transp, stat_struct *stats, const char *genome_xml,
+                        unsigned char **png, size_t *png_len);
+
+/* Kernel time (ms, CUDA events) of the calling thread's last PNG encode. */
+int flam3gpu_png_last_ms(double *encode_ms);
 
 /* Last error message of the calling thread ("" if none). */
 const char *flam3gpu_last_error(void);

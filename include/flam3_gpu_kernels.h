@@ -20,13 +20,19 @@ extern "C" {
  *   hist_out : receives the last batch's histogram in the same layout.
  *   accum_out: receives the accumulator before the spatial filter
  *              (hist_h x hist_w x 4 doubles).
- *   hist_w, hist_h: set by the call. */
+ *   hist_w, hist_h: set by the call.
+ *   keep_on_device: the packed image stays in the calling thread's device
+ *              buffer for a following device step (flam3gpu_render_png);
+ *              `out` is not written and may be NULL.
+ *   image_w, image_h: the packed image's size, set by the call. */
 typedef struct {
   const double *hist_in;
   double *hist_out;
   double *accum_out;
   int hist_w, hist_h;
-  int reserved[6];
+  int keep_on_device;
+  int image_w, image_h;
+  int reserved[3];
 } flam3gpu_render_io;
 
 /* flam3gpu_render with optional parity inputs/outputs (io may be NULL). */

@@ -68,6 +68,9 @@ def oracle(fast=False):
     lib.f3o_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     lib.f3o_set_interpolator.argtypes = [C.c_void_p]
     lib.f3o_set_interpolator.restype = None
+    lib.oracle_png_filter.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    lib.oracle_png_filter.restype = C.c_longlong
+    lib.oracle_png_unfilter.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
     _cache[key] = lib
     return lib
 
@@ -218,3 +221,22 @@ def ref_apply_xform(genome, fn, points, words):
         bad[k] = lib.apply_xform(C.byref(g), fn, p, qq, C.byref(rc))
         q[k] = list(qq)
     return q, bad
+
+
+def png_filter(img, fast=False):
+    """The filtered stream write_png's libpng call deflates (oracle restatement)."""
+    img = np.ascontiguousarray(img)
+    h, w, nchan = img.shape
+    bpc = img.dtype.itemsize
+    F = np.zeros(h * (1 + w * nchan * bpc), np.uint8)
+    oracle(fast).oracle_png_filter(img.ctypes.data, w, h, nchan, bpc, F.ctypes.data)
+    return F
+
+
+def png_unfilter(F, shape, dtype):
+    h, w, nchan = shape
+    out = np.zeros(shape, dtype)
+    F = np.ascontiguousarray(F, dtype=np.uint8)
+    if oracle().oracle_png_unfilter(F.ctypes.data, w, h, nchan, np.dtype(dtype).itemsize, out.ctypes.data):
+        raise ValueError("bad PNG filter type")
+    return out
