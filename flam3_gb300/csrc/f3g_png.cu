@@ -72,9 +72,16 @@ __global__ void __launch_bounds__(NT) k_png_deflate(SegArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SegShared &S = *reinterpret_cast<SegShared *>(smem_raw);
   const int seg = blockIdx.x, tid = threadIdx.x;
-  phase_init(S, A, tid);
+  phase_init(S, A, seg, tid);
+  __syncthreads();
+  phase_window(S, A, seg, tid);
   __syncthreads();
   phase_hist(S, A, seg, tid);
+  __syncthreads();
+  phase_keys(S, tid);
+  __syncthreads();
+  sort_keys(S, tid);
+  phase_bounds(S, tid);
   __syncthreads();
   phase_rank(S, tid);
   __syncthreads();
@@ -82,8 +89,15 @@ __global__ void __launch_bounds__(NT) k_png_deflate(SegArgs A) {
   __syncthreads();
   phase_codes(S, tid);
   __syncthreads();
-  phase_header(S, tid);
+  phase_rle_count(S, tid);
   __syncthreads();
+  phase_rle_scan(S, tid);
+  __syncthreads();
+  phase_rle_write(S, tid);
+  __syncthreads();
+  phase_cl_code(S, tid);
+  __syncthreads();
+  phase_hdr_bits(S, tid);
   phase_count(S, A, seg, tid);
   __syncthreads();
   phase_layout(S, A, seg, tid);
@@ -92,12 +106,20 @@ __global__ void __launch_bounds__(NT) k_png_deflate(SegArgs A) {
   __syncthreads();
   uint32_t q;
   phase_crc_parts(S, tid, q);
-  if (tid == 0) {
-    S.crc_x[0] = gf2_xpow(8ull * q);
-    for (int l = 0; l + 1 < 8; l++) S.crc_x[l + 1] = gf2_mult(S.crc_x[l], S.crc_x[l]);
+  if (tid < 32) {
+    /* warp 0: the shifts of the combine levels and of the whole chunk */
+    uint32_t x = xpow8_warp(q);
+    const uint32_t xn = xpow8_warp(4 + S.nbytes);
+    if (tid == 0) {
+      S.crc_xn = xn;
+      for (int l = 0; l < LOG_NT; l++) {
+        S.crc_x[l] = x;
+        x = gf2_mult(x, x);
+      }
+    }
   }
   __syncthreads();
-  for (int l = 0; l < 8; l++) {
+  for (int l = 0; l < LOG_NT; l++) {
     phase_crc_level(S, tid, l, S.crc_x[l]);
     __syncthreads();
   }
@@ -204,7 +226,8 @@ int f3g_png_segments(int w, int h, int nchan, int bpc) {
 size_t f3g_png_work_bytes(int w, int h, int nchan, int bpc) {
   const long long fb = f3g_png_filtered_bytes(w, h, nchan, bpc);
   const long long ns = f3g_png_segments(w, h, nchan, bpc);
-  return (size_t)(((fb + 255) / 256) * 256 + ns * STAGE + ns * (long long)sizeof(SegMeta));
+  return (size_t)(((fb + 255) / 256) * 256 + ns * STAGE + ns * (long long)sizeof(SegMeta) +
+                  ns * (long long)SEG * 2);
 }
 
 /* the IDAT chunks' bytes, at most */
@@ -225,6 +248,7 @@ int f3g_png_encode_idat(const void *d_img, int w, int h, int nchan, int bpc, voi
   uint8_t *F = (uint8_t *)d_work;
   uint8_t *stage = F + ((fb + 255) / 256) * 256;
   SegMeta *meta = (SegMeta *)(stage + (size_t)ns * STAGE);
+  uint16_t *tokens = (uint16_t *)(meta + ns);
   static int attr_set = 0;
   const int smem = (int)sizeof(SegShared);
   if (!attr_set) {
@@ -241,6 +265,7 @@ int f3g_png_encode_idat(const void *d_img, int w, int h, int nchan, int bpc, voi
   A.nseg = ns;
   A.stage = stage;
   A.meta = meta;
+  A.tokens = tokens;
   k_png_deflate<<<ns, NT, smem, st>>>(A);
   k_png_assemble<<<ns, NT, 0, st>>>(stage, meta, ns, fb, (uint8_t *)d_idat, d_len);
   return cudaGetLastError() == cudaSuccess ? 0 : 3;

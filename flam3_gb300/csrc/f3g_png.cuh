@@ -24,6 +24,7 @@
  */
 #pragma once
 #include <stdint.h>
+#include <string.h>
 
 #ifdef __CUDACC__
 #define PNG_HD __host__ __device__ __forceinline__
@@ -33,14 +34,17 @@
 
 namespace f3gpng {
 
-constexpr int SEG = 32768;          /* filtered bytes per segment (one CTA) */
+constexpr int SEG = 16384;          /* filtered bytes per segment (one CTA) */
 constexpr int NT = 256;             /* threads per CTA */
+constexpr int LOG_NT = 8;
 constexpr int SUB = SEG / NT;       /* bytes parsed by one thread */
 constexpr int MIN_MATCH = 4;        /* shortest match emitted (3 is legal) */
 constexpr int MAX_MATCH = 258;
-constexpr int WINDOW = 32768;
+constexpr int WINDOW = 32768;       /* deflate's largest distance */
+constexpr int LOOKBACK = 16384;     /* bytes before a segment that its matches may reach */
 constexpr int NLIT = 286, NDIST = 30, NCL = 19;
-constexpr int MAXD = 4;             /* candidate distances */
+constexpr int MAXD = 9;             /* fixed candidate distances */
+constexpr int WT_BITS = 11;         /* window table: 4-byte hash -> latest position */
 constexpr int OUT_BYTES = SEG + 64; /* a segment's deflate output, at most */
 constexpr int STAGE = OUT_BYTES;    /* per-segment staging stride (bytes) */
 constexpr uint32_t CRC_POLY = 0xEDB88320u;
@@ -76,6 +80,14 @@ PNG_HD void atomic_or_u32(uint32_t *p, uint32_t v) {
   atomicOr(p, v);
 #else
   *p |= v;
+#endif
+}
+
+PNG_HD void atomic_max_u32(uint32_t *p, uint32_t v) {
+#ifdef __CUDA_ARCH__
+  atomicMax(p, v);
+#else
+  if (v > *p) *p = v;
 #endif
 }
 
@@ -119,30 +131,99 @@ PNG_HD void dist_code(int d, int &sym, int &next, int &extra) {
   extra = m & ((1 << (n - 1)) - 1);
 }
 
-/* Greedy parse of F[beg, end): at each position the longest run equal to
- * the bytes at one of the candidate distances (no match reaches past end),
- * a match when it is at least MIN_MATCH long, else a literal. */
+/* multiplicative hash of the 4 bytes at p (Knuth's golden-ratio constant) */
+PNG_HD uint32_t hash4(const uint8_t *p) {
+  const uint32_t v = (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+  return (v * 2654435761u) >> (32 - WT_BITS);
+}
+
+/* where a parse looks for matches: fixed distances (neighbouring pixels and
+ * rows) and the latest earlier occurrence of the next 4 bytes in the 32 KB
+ * before the segment (wtab[h] = position - wbase + 1, 0 = none) */
+struct Cands {
+  const int *dist;
+  int nd;
+  const uint32_t *wtab;
+  long long wbase, total;
+};
+
+/* the 4 bytes at w[pos] as a little-endian word (w 4-byte aligned; may read
+ * up to 3 bytes past the valid data, which the caller masks by length) */
+PNG_HD uint32_t load32u(const uint8_t *w, int pos) {
+#ifdef __CUDA_ARCH__
+  const uint32_t *q = reinterpret_cast<const uint32_t *>(w);
+  return __funnelshift_r(q[pos >> 2], q[(pos >> 2) + 1], (pos & 3) * 8);
+#else
+  uint32_t v;
+  memcpy(&v, w + pos, 4);
+  return v;
+#endif
+}
+
+PNG_HD int ctz32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+  return __ffs((int)x) - 1;
+#else
+  return __builtin_ctz(x);
+#endif
+}
+
+/* bytes equal at a and a - d, up to maxlen, compared a word at a time */
+PNG_HD int match_len(const uint8_t *F, int a, int d, int maxlen) {
+  int L = 0;
+  while (L < maxlen) {
+    const uint32_t x = load32u(F, a + L) ^ load32u(F, a - d + L);
+    if (x) {
+      L += ctz32(x) >> 3;
+      break;
+    }
+    L += 4;
+  }
+  return L < maxlen ? L : maxlen;
+}
+
+/* longest match at p among the candidates, not reaching past end; the
+ * search stops at the first match of the greatest possible length */
+PNG_HD int best_match(const uint8_t *F, long long p, long long end, const Cands &C, int &bd) {
+  const int maxlen = (int)((end - p) < MAX_MATCH ? (end - p) : MAX_MATCH);
+  int bl = 0;
+  bd = 0;
+  const int ip = (int)p;
+  const uint8_t x0 = F[ip];
+  for (int k = 0; k < C.nd && bl < maxlen; k++) {
+    const int d = C.dist[k];
+    if (d > ip || F[ip - d] != x0) continue;
+    const int L = match_len(F, ip, d, maxlen);
+    if (L > bl) bl = L, bd = d;
+  }
+  if (bl < maxlen && p + 4 <= C.total) {
+    const uint32_t v = C.wtab[hash4(F + ip)];
+    if (v) {
+      const long long d = p - (C.wbase + (long long)v - 1);
+      if (d >= 1 && d <= WINDOW && F[ip - d] == x0) {
+        const int L = match_len(F, ip, (int)d, maxlen);
+        if (L > bl) bl = L, bd = (int)d;
+      }
+    }
+  }
+  return bl;
+}
+
+/* Greedy parse of F[beg, end): the longest candidate match at each
+ * position when it is at least MIN_MATCH long, else a literal.  (One step of
+ * lazy evaluation, as zlib does, gains under 1 % on rendered images for
+ * twice the search.) */
 template <class Sink>
-PNG_HD void parse(const uint8_t *F, long long beg, long long end, const int *dist, int nd, Sink &s) {
+PNG_HD void parse(const uint8_t *F, long long beg, long long end, const Cands &C, Sink &s) {
   long long p = beg;
   while (p < end) {
-    const int maxlen = (int)((end - p) < MAX_MATCH ? (end - p) : MAX_MATCH);
-    int bl = 0, bd = 0;
-    const uint8_t x0 = F[p];
-    for (int k = 0; k < nd; k++) {
-      const int d = dist[k];
-      if ((long long)d > p) continue;
-      const uint8_t *a = F + p, *b = F + p - d;
-      if (b[0] != x0) continue;
-      int L = 1;
-      while (L < maxlen && a[L] == b[L]) L++;
-      if (L > bl) bl = L, bd = d;
-    }
+    int bd;
+    const int bl = best_match(F, p, end, C, bd);
     if (bl >= MIN_MATCH) {
       s.match(bl, bd);
       p += bl;
     } else {
-      s.literal(x0);
+      s.literal(F[p]);
       p++;
     }
   }
@@ -150,44 +231,100 @@ PNG_HD void parse(const uint8_t *F, long long beg, long long end, const int *dis
 
 /* ---- shared state of one segment's CTA ---- */
 
-struct HuffScratch {
-  uint16_t sorted[NLIT]; /* used symbols, ascending frequency */
-  uint32_t wi[NLIT];     /* internal node weights */
-  uint16_t par_leaf[NLIT], par_int[NLIT];
-  uint8_t depth[NLIT];
-  int nused;
+template <int N>
+struct HuffScratchT {
+  uint16_t sorted[N]; /* used symbols, ascending frequency */
+  uint32_t wl[N];     /* their frequencies, in that order */
+  uint32_t wi[N];     /* internal node weights */
+  uint16_t par_leaf[N], par_int[N];
+  uint8_t depth[N];
+  uint32_t first[16]; /* first canonical code of each length */
+  uint32_t nused;
 };
+using HuffScratch = HuffScratchT<NLIT>;
+using HuffScratchSmall = HuffScratchT<32>; /* distances (30), code lengths (19) */
 
 struct SegShared {
-  uint32_t out[OUT_BYTES / 4];
+  alignas(16) uint8_t win[LOOKBACK + SEG]; /* F[w0, se): the segment and the bytes before it */
+  union {
+    uint32_t out[OUT_BYTES / 4];
+    unsigned long long keys[1024]; /* symbol sort keys, before the output exists */
+  };
   uint32_t hist_lit[NLIT], hist_dist[NDIST], hist_cl[NCL];
   uint16_t code_lit[NLIT], code_dist[NDIST], code_cl[NCL]; /* bit-reversed */
   uint8_t len_lit[NLIT], len_dist[NDIST], len_cl[NCL];
   uint8_t cl_sym[NLIT + NDIST], cl_extra[NLIT + NDIST];
-  HuffScratch hs[2];
+  HuffScratch hs0;      /* literal/length alphabet */
+  HuffScratchSmall hs1; /* distance alphabet, then the code-length code */
   uint32_t crc_table[256];
-  uint32_t tbits[NT];           /* per-thread token bits, then their offsets */
-  uint32_t crc_part[NT];
+  union {
+    uint32_t tbits[NT];         /* per-thread token bits, then their offsets */
+    uint32_t crc_part[NT];      /* per-thread CRC registers, after the block is out */
+  };
+  int ntok[NT];                 /* per-thread token entries */
   uint32_t crc_x[8];            /* x^(8 q 2^l) mod the CRC polynomial */
+  uint32_t crc_xn;              /* x^(8 n), n = 4 + the segment's bytes */
   uint32_t a1[NT], a2[NT], alen[NT]; /* Adler-32 partial sums per thread */
   int ncl, hlit, hdist, hclen;
+  uint32_t lit_end, dist_end;   /* one past the last nonzero length */
+  uint32_t dist_first, dist_last; /* the distance keys' range after the sort */
   uint32_t hdr_bits, body_bits, nbytes, mode;
   int dist[MAXD], nd;
+  uint32_t wtab[1 << WT_BITS];
+  long long w0;                 /* stream position of win[0] */
+  int wlen;                     /* bytes staged in win */
+  /* the parse works in positions relative to w0 */
+  PNG_HD Cands cands() const { return Cands{dist, nd, wtab, 0, wlen}; }
 };
 
 /* ---- sinks of the parse ---- */
 
 struct HistSink {
   SegShared *S;
-  PNG_HD void literal(uint8_t v) { atomic_add_u32(&S->hist_lit[v], 1); }
+  uint16_t *tok;
+  int n;
+  PNG_HD void literal(uint8_t v) {
+    atomic_add_u32(&S->hist_lit[v], 1);
+    tok[(size_t)(n++) * NT] = v;
+  }
   PNG_HD void match(int L, int d) {
-    int s, n, e;
-    len_code(L, s, n, e);
+    int s, nx, e;
+    len_code(L, s, nx, e);
     atomic_add_u32(&S->hist_lit[s], 1);
-    dist_code(d, s, n, e);
+    dist_code(d, s, nx, e);
     atomic_add_u32(&S->hist_dist[s], 1);
+    tok[(size_t)(n++) * NT] = (uint16_t)(256 + L - 3);
+    tok[(size_t)(n++) * NT] = (uint16_t)(d - 1);
   }
 };
+
+/* replays a thread's tokens into a sink */
+template <class Sink>
+PNG_HD void replay(const uint16_t *tok, int n, Sink &s) {
+  constexpr int B = 8; /* entries loaded ahead, independent loads */
+  int i = 0;
+  while (i < n) {
+    uint16_t t[B];
+    const int m = n - i < B ? n - i : B;
+#pragma unroll
+    for (int k = 0; k < B; k++) t[k] = k < m ? tok[(size_t)(i + k) * NT] : 0;
+    int j = 0;
+#pragma unroll
+    for (int k = 0; k < B; k++) {
+      if (k != j || j >= m) continue;
+      const int v = t[k];
+      if (v < 256) {
+        s.literal((uint8_t)v);
+        j = k + 1;
+      } else {
+        const int d = k + 1 < m ? t[k + 1] : tok[(size_t)(i + k + 1) * NT];
+        s.match(v - 253, d + 1);
+        j = k + 2;
+      }
+    }
+    i += j;
+  }
+}
 
 struct CountSink {
   const SegShared *S;
@@ -250,19 +387,6 @@ struct EmitSink {
 
 /* rank of symbol `sym` among the used symbols by (frequency, symbol); run
  * by every thread for its symbols, fills h.sorted */
-PNG_HD void rank_symbols(const uint32_t *freq, int n, HuffScratch &h, int tid, int nthreads) {
-  for (int s = tid; s < n; s += nthreads) {
-    const uint32_t f = freq[s];
-    if (!f) continue;
-    int r = 0;
-    for (int j = 0; j < n; j++) {
-      const uint32_t g = freq[j];
-      r += (g && (g < f || (g == f && j < s))) ? 1 : 0;
-    }
-    h.sorted[r] = (uint16_t)s;
-  }
-}
-
 PNG_HD int count_used(const uint32_t *freq, int n) {
   int m = 0;
   for (int s = 0; s < n; s++) m += freq[s] ? 1 : 0;
@@ -271,87 +395,91 @@ PNG_HD int count_used(const uint32_t *freq, int n) {
 
 /* Huffman code lengths limited to maxbits, forming a complete code (Kraft
  * sum exactly 1) whenever at least two symbols are used; one used symbol
- * gets length 1.  h.sorted must hold the used symbols in ascending
- * frequency.  One thread. */
-PNG_HD void huff_lengths(const uint32_t *freq, int n, int maxbits, HuffScratch &h, uint8_t *len) {
-  for (int s = 0; s < n; s++) len[s] = 0;
-  const int m = count_used(freq, n);
-  h.nused = m;
-  if (m == 0) return;
+ * gets length 1.  h.sorted / h.wl / h.nused hold the used symbols in
+ * ascending frequency (phase_rank); len must be zero on entry.  Also
+ * leaves the first canonical code of each length in h.first.  One thread. */
+template <class H>
+PNG_HD void huff_lengths(int maxbits, H &h, uint8_t *len) {
+  const int m = (int)h.nused;
+  int bl[16];
+  for (int b = 0; b < 16; b++) bl[b] = 0;
   if (m == 1) {
     len[h.sorted[0]] = 1;
-    return;
-  }
-  /* two-queue construction: leaves in ascending order, internal nodes are
-   * created in ascending order too */
-  int i = 0, j = 0;
-  for (int t = 0; t < m - 1; t++) {
-    uint32_t w = 0;
-    for (int pick = 0; pick < 2; pick++) {
-      if (i < m && (j >= t || freq[h.sorted[i]] <= h.wi[j])) {
-        w += freq[h.sorted[i]];
-        h.par_leaf[i++] = (uint16_t)t;
-      } else {
-        w += h.wi[j];
-        h.par_int[j++] = (uint16_t)t;
+    bl[1] = 1;
+  } else if (m >= 2) {
+    /* two-queue construction: leaves in ascending order, internal nodes
+     * are created in ascending order too */
+    int i = 0, j = 0;
+    uint32_t wleaf = h.wl[0];
+    for (int t = 0; t < m - 1; t++) {
+      uint32_t w = 0;
+      for (int pick = 0; pick < 2; pick++) {
+        if (i < m && (j >= t || wleaf <= h.wi[j])) {
+          w += wleaf;
+          h.par_leaf[i++] = (uint16_t)t;
+          wleaf = i < m ? h.wl[i] : 0;
+        } else {
+          w += h.wi[j];
+          h.par_int[j++] = (uint16_t)t;
+        }
       }
+      h.wi[t] = w;
     }
-    h.wi[t] = w;
+    /* depths: the root is the last internal node */
+    uint8_t *dint = h.depth;
+    dint[m - 2] = 0;
+    for (int t = m - 3; t >= 0; t--) {
+      const int d = dint[h.par_int[t]] + 1;
+      dint[t] = (uint8_t)(d < 255 ? d : 255);
+    }
+    for (int k = 0; k < m; k++) {
+      int d = dint[h.par_leaf[k]] + 1;
+      if (d > maxbits) d = maxbits;
+      bl[d]++;
+    }
+    /* Kraft sum in units of 2^-maxbits; lengthen codes while it is over
+     * one, then shorten the deepest ones while it is under */
+    const long long full = 1ll << maxbits;
+    long long K = 0;
+    for (int b = 1; b <= maxbits; b++) K += (long long)bl[b] << (maxbits - b);
+    while (K > full) {
+      int b = maxbits - 1;
+      while (b > 0 && bl[b] == 0) b--;
+      bl[b]--;
+      bl[b + 1]++;
+      K -= 1ll << (maxbits - b - 1);
+    }
+    while (K < full) {
+      int b = maxbits;
+      while (b > 1 && (bl[b] == 0 || (1ll << (maxbits - b)) > full - K)) b--;
+      if (b <= 1) break; /* cannot happen: K and full are multiples of the deepest step */
+      bl[b]--;
+      bl[b - 1]++;
+      K += 1ll << (maxbits - b);
+    }
+    /* the least frequent symbols take the longest codes */
+    int k = 0;
+    for (int b = maxbits; b >= 1; b--)
+      for (int c = 0; c < bl[b]; c++) len[h.sorted[k++]] = (uint8_t)b;
   }
-  /* depths: the root is the last internal node */
-  uint8_t *dint = h.depth; /* internal node depths, reused */
-  dint[m - 2] = 0;
-  for (int t = m - 3; t >= 0; t--) dint[t] = (uint8_t)(dint[h.par_int[t]] + 1 < 255 ? dint[h.par_int[t]] + 1 : 255);
-  int bl[33];
-  for (int b = 0; b <= 32; b++) bl[b] = 0;
-  for (int k = 0; k < m; k++) {
-    int d = dint[h.par_leaf[k]] + 1;
-    if (d > maxbits) d = maxbits;
-    bl[d]++;
+  uint32_t code = 0;
+  h.first[0] = 0;
+  for (int b = 1; b < 16; b++) {
+    code = (code + (b > 1 ? bl[b - 1] : 0)) << (b > 1 ? 1 : 0);
+    h.first[b] = code;
   }
-  /* Kraft sum in units of 2^-maxbits; lengthen codes while it is over one,
-   * then shorten the deepest ones while it is under */
-  const long long full = 1ll << maxbits;
-  long long K = 0;
-  for (int b = 1; b <= maxbits; b++) K += (long long)bl[b] << (maxbits - b);
-  while (K > full) {
-    int b = maxbits - 1;
-    while (b > 0 && bl[b] == 0) b--;
-    bl[b]--;
-    bl[b + 1]++;
-    K -= 1ll << (maxbits - b - 1);
-  }
-  while (K < full) {
-    int b = maxbits;
-    while (b > 1 && (bl[b] == 0 || (1ll << (maxbits - b)) > full - K)) b--;
-    if (b <= 1) break; /* cannot happen: see the multiple-of argument */
-    bl[b]--;
-    bl[b - 1]++;
-    K += 1ll << (maxbits - b);
-  }
-  /* the least frequent symbols take the longest codes */
-  int k = 0;
-  for (int b = maxbits; b >= 1; b--)
-    for (int c = 0; c < bl[b]; c++) len[h.sorted[k++]] = (uint8_t)b;
 }
 
-/* canonical codes (RFC 1951 3.2.2), stored bit-reversed for LSB-first output */
-PNG_HD void canonical_codes(const uint8_t *len, int n, uint16_t *code, int tid, int nthreads) {
+/* canonical codes (RFC 1951 3.2.2), stored bit-reversed for LSB-first
+ * output: the first code of the symbol's length plus its rank among the
+ * earlier symbols of that length */
+PNG_HD void canonical_codes(const uint8_t *len, int n, const uint32_t *first, uint16_t *code, int tid,
+                            int nthreads) {
   for (int s = tid; s < n; s += nthreads) {
     const int L = len[s];
-    if (!L) {
-      code[s] = 0;
-      continue;
-    }
-    /* first code of length L: codes of all shorter lengths, doubled per step */
     uint32_t c = 0;
-    for (int b = 1; b < L; b++) {
-      int cnt = 0;
-      for (int j = 0; j < n; j++) cnt += len[j] == b ? 1 : 0;
-      c = (c + cnt) << 1;
-    }
-    for (int j = 0; j < s; j++) c += len[j] == L ? 1 : 0;
-    code[s] = (uint16_t)rev_bits(c, L);
+    for (int j = 0; j < s; j++) c += len[j] == L ? 1u : 0u;
+    code[s] = L ? (uint16_t)rev_bits(first[L] + c, L) : 0;
   }
 }
 
@@ -366,16 +494,59 @@ PNG_HD uint32_t gf2_mult(uint32_t a, uint32_t b) {
   return p;
 }
 
-/* x^e modulo the CRC polynomial, reflected */
-PNG_HD uint32_t gf2_xpow(unsigned long long e) {
-  uint32_t r = 0x80000000u, base = 0x40000000u;
-  while (e) {
-    if (e & 1) r = gf2_mult(r, base);
-    base = gf2_mult(base, base);
-    e >>= 1;
+/* x^(8 * 2^k) modulo the CRC polynomial (reflected), k = 0..31: the
+ * shift of a CRC register over 2^k zero bytes */
+struct X8Table {
+  uint32_t v[32];
+};
+
+constexpr uint32_t cx_mult(uint32_t a, uint32_t b) {
+  uint32_t p = 0;
+  for (int i = 0; i < 32; i++) {
+    if (a & (0x80000000u >> i)) p ^= b;
+    b = (b & 1u) ? (b >> 1) ^ CRC_POLY : b >> 1;
   }
+  return p;
+}
+
+constexpr X8Table make_x8() {
+  X8Table t{};
+  uint32_t p = 0x00800000u; /* x^8 */
+  for (int k = 0; k < 32; k++) {
+    t.v[k] = p;
+    p = cx_mult(p, p);
+  }
+  return t;
+}
+
+#ifdef __CUDACC__
+__constant__ X8Table c_x8 = make_x8();
+#endif
+
+/* x^(8 n) modulo the CRC polynomial, one thread */
+PNG_HD uint32_t xpow8(uint32_t n) {
+#ifdef __CUDA_ARCH__
+  const X8Table &t = c_x8;
+#else
+  static constexpr X8Table t = make_x8();
+#endif
+  uint32_t r = 0x80000000u;
+  for (int k = 0; k < 32; k++)
+    if ((n >> k) & 1u) r = gf2_mult(r, t.v[k]);
   return r;
 }
+
+#ifdef __CUDACC__
+/* the same over a whole warp (every lane gets the product): lane k holds
+ * the factor of bit k, then a butterfly of products */
+__device__ __forceinline__ uint32_t xpow8_warp(uint32_t n) {
+  const int lane = threadIdx.x & 31;
+  uint32_t f = ((n >> lane) & 1u) ? c_x8.v[lane] : 0x80000000u;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) f = gf2_mult(f, __shfl_xor_sync(0xffffffffu, f, o));
+  return f;
+}
+#endif
 
 /* transmission order of the code-length code lengths (RFC 1951 3.2.7) */
 PNG_HD int cl_order(int k) {
@@ -392,7 +563,13 @@ struct SegArgs {
   int nseg;
   uint8_t *stage;     /* nseg x STAGE bytes */
   SegMeta *meta;
+  uint16_t *tokens;   /* nseg x SEG parse tokens, interleaved over the threads */
 };
+
+/* A thread's parse tokens: a literal is one entry (the byte), a match two
+ * (256 + length - 3, then distance - 1); never more entries than bytes.
+ * Entry k of thread t sits at k * NT + t of the segment's area. */
+PNG_HD uint16_t *thread_tokens(const SegArgs &A, int seg, int tid) { return A.tokens + (size_t)seg * SEG + tid; }
 
 PNG_HD void seg_range(const SegArgs &A, int seg, long long &b, long long &e) {
   b = (long long)seg * SEG;
@@ -409,19 +586,39 @@ PNG_HD void sub_range(const SegArgs &A, int seg, int tid, long long &b, long lon
 }
 
 /* phase 0: clear, CRC table, candidate distances */
-PNG_HD void phase_init(SegShared &S, const SegArgs &A, int tid) {
-  for (int i = tid; i < OUT_BYTES / 4; i += NT) S.out[i] = 0;
-  for (int i = tid; i < NLIT; i += NT) S.hist_lit[i] = 0;
-  for (int i = tid; i < NDIST; i += NT) S.hist_dist[i] = 0;
-  for (int i = tid; i < NCL; i += NT) S.hist_cl[i] = 0;
+PNG_HD void phase_init(SegShared &S, const SegArgs &A, int seg, int tid) {
+  for (int i = tid; i < NLIT; i += NT) S.hist_lit[i] = 0, S.len_lit[i] = 0;
+  for (int i = tid; i < NDIST; i += NT) S.hist_dist[i] = 0, S.len_dist[i] = 0;
+  for (int i = tid; i < NCL; i += NT) S.hist_cl[i] = 0, S.len_cl[i] = 0;
   for (int i = tid; i < 256; i += NT) {
     uint32_t c = (uint32_t)i;
     for (int k = 0; k < 8; k++) c = (c & 1u) ? (c >> 1) ^ CRC_POLY : c >> 1;
     S.crc_table[i] = c;
   }
+  for (int i = tid; i < (1 << WT_BITS); i += NT) S.wtab[i] = 0;
+  /* stage F[w0, se) (w0 and F are 16-byte aligned: segments start at
+   * multiples of SEG) */
+  const long long sb = (long long)seg * SEG;
+  const long long se = sb + SEG < A.total ? sb + SEG : A.total;
+  const long long w0 = sb - LOOKBACK > 0 ? sb - LOOKBACK : 0;
+  const int n = (int)(se - w0);
+#ifdef __CUDA_ARCH__
+  const uint4 *src = reinterpret_cast<const uint4 *>(A.F + w0);
+  uint4 *dst = reinterpret_cast<uint4 *>(S.win);
+  for (int i = tid; i < n / 16; i += NT) dst[i] = src[i];
+  for (int i = (n / 16) * 16 + tid; i < n; i += NT) S.win[i] = A.F[w0 + i];
+#else
+  if (tid == 0) memcpy(S.win, A.F + w0, (size_t)n);
+#endif
   if (tid == 0) {
+    S.w0 = w0;
+    S.wlen = n;
+    S.hs0.nused = S.hs1.nused = 0;
+    S.dist_first = S.dist_last = 0;
+    S.lit_end = S.dist_end = 0;
     int nd = 0;
-    const int cand[MAXD] = {1, A.bpp, A.stride, 2 * A.bpp};
+    const int cand[MAXD] = {1,          A.bpp,          A.stride, 2 * A.bpp, A.stride - A.bpp,
+                            A.stride + A.bpp, 3 * A.bpp, 4 * A.bpp, 2 * A.stride};
     for (int k = 0; k < MAXD; k++) {
       const int d = cand[k];
       bool dup = d < 1 || d > WINDOW;
@@ -432,16 +629,36 @@ PNG_HD void phase_init(SegShared &S, const SegArgs &A, int tid) {
   }
 }
 
+/* phase 0b: the window table over the look-back before the segment; the
+ * maximum is order-independent, so the table is the same on every run */
+PNG_HD void phase_window(SegShared &S, const SegArgs &A, int seg, int tid) {
+  long long sb, se;
+  seg_range(A, seg, sb, se);
+  (void)se;
+  const int nb = (int)(sb - S.w0); /* window bytes before the segment */
+  for (int q = tid; q < nb && q + 4 <= S.wlen; q += NT) {
+    const uint32_t v = (uint32_t)(q + 1);
+#ifdef __CUDA_ARCH__
+    atomicMax(&S.wtab[hash4(S.win + q)], v);
+#else
+    uint32_t &t = S.wtab[hash4(S.win + q)];
+    if (v > t) t = v;
+#endif
+  }
+}
+
 /* phase 1: symbol histogram and Adler-32 partial sums */
 PNG_HD void phase_hist(SegShared &S, const SegArgs &A, int seg, int tid) {
   long long b, e;
   sub_range(A, seg, tid, b, e);
-  HistSink hsink{&S};
-  parse(A.F, b, e, S.dist, S.nd, hsink);
+  HistSink hsink{&S, thread_tokens(A, seg, tid), 0};
+  const long long rb = b - S.w0, re = e - S.w0;
+  parse(S.win, rb, re, S.cands(), hsink);
+  S.ntok[tid] = hsink.n;
   unsigned long long s1 = 0, s2 = 0;
-  for (long long p = b; p < e; p++) {
-    s1 += A.F[p];
-    s2 += (unsigned long long)(e - p) * A.F[p];
+  for (long long p = rb; p < re; p++) {
+    s1 += S.win[p];
+    s2 += (unsigned long long)(re - p) * S.win[p];
   }
   S.a1[tid] = (uint32_t)s1;
   S.a2[tid] = (uint32_t)s2;
@@ -449,110 +666,233 @@ PNG_HD void phase_hist(SegShared &S, const SegArgs &A, int seg, int tid) {
   if (tid == 0) atomic_add_u32(&S.hist_lit[256], 1); /* end of block */
 }
 
-/* phase 2: order the used symbols of both alphabets */
+/* phase 2a: sort keys of both alphabets' symbols, (alphabet, frequency,
+ * symbol) ascending with unused symbols last */
+PNG_HD void phase_keys(SegShared &S, int tid) {
+  for (int i = tid; i < 1024; i += NT) {
+    unsigned long long k = ~0ull;
+    if (i < NLIT && S.hist_lit[i]) k = ((unsigned long long)S.hist_lit[i] << 16) | (unsigned)i;
+    if (i >= 512 && i - 512 < NDIST && S.hist_dist[i - 512])
+      k = (1ull << 63) | ((unsigned long long)S.hist_dist[i - 512] << 16) | (unsigned)(i - 512);
+    S.keys[i] = k;
+  }
+}
+
+#ifdef __CUDACC__
+/* phase 2b on the device: bitonic sort of the 1024 keys by the whole CTA */
+__device__ __forceinline__ void sort_keys(SegShared &S, int tid) {
+  for (int k = 2; k <= 1024; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = tid; i < 1024; i += NT) {
+        const int l = i ^ j;
+        if (l > i) {
+          const unsigned long long a = S.keys[i], b = S.keys[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) S.keys[i] = b, S.keys[l] = a;
+        }
+      }
+      __syncthreads();
+    }
+}
+#endif
+
+/* phase 2c: how many symbols each alphabet uses (where the sorted keys
+ * change alphabet or become unused) */
+PNG_HD void phase_bounds(SegShared &S, int tid) {
+  for (int i = tid; i < 1024; i += NT) {
+    const unsigned long long k = S.keys[i], n = i + 1 < 1024 ? S.keys[i + 1] : ~0ull;
+    const int ka = k == ~0ull ? 2 : (int)(k >> 63), na = n == ~0ull ? 2 : (int)(n >> 63);
+    if (i == 0 && ka != 0) S.hs0.nused = 0;
+    if (ka == 0 && na != 0) S.hs0.nused = (uint32_t)(i + 1);
+    if (ka != 1 && na == 1) S.dist_first = (uint32_t)(i + 1);
+    if (i == 0 && ka == 1) S.dist_first = 0;
+    if (ka == 1 && na != 1) S.dist_last = (uint32_t)(i + 1);
+  }
+}
+
+/* phase 2d: the used symbols of each alphabet in ascending order */
 PNG_HD void phase_rank(SegShared &S, int tid) {
-  rank_symbols(S.hist_lit, NLIT, S.hs[0], tid, NT);
-  rank_symbols(S.hist_dist, NDIST, S.hs[1], tid, NT);
+  if (tid == 0) S.hs1.nused = S.dist_last > S.dist_first ? S.dist_last - S.dist_first : 0;
+  for (int i = tid; i < 1024; i += NT) {
+    const unsigned long long k = S.keys[i];
+    if (k == ~0ull) continue;
+    const int a = (int)(k >> 63);
+    /* literal/length keys come first: a distance key's rank is i minus them */
+    const uint16_t sym = (uint16_t)(k & 0xFFFF);
+    const uint32_t f = (uint32_t)((k >> 16) & 0x7FFFFFFFull);
+    if (a) {
+      const int r = i - (int)S.dist_first;
+      S.hs1.sorted[r] = sym, S.hs1.wl[r] = f;
+    } else {
+      S.hs0.sorted[i] = sym, S.hs0.wl[i] = f;
+    }
+  }
 }
 
 /* phase 3: code lengths (thread 0: literal/length, thread 32: distance) */
 PNG_HD void phase_lengths(SegShared &S, int tid) {
-  if (tid == 0) huff_lengths(S.hist_lit, NLIT, 15, S.hs[0], S.len_lit);
+  if (tid == 0) huff_lengths(15, S.hs0, S.len_lit);
   if (tid == 32) {
-    huff_lengths(S.hist_dist, NDIST, 15, S.hs[1], S.len_dist);
     /* no matches: one distance code of one bit (RFC 1951 3.2.7) */
-    if (S.hs[1].nused == 0) S.len_dist[0] = 1;
+    if (S.hs1.nused == 0) S.hs1.nused = 1, S.hs1.sorted[0] = 0;
+    huff_lengths(15, S.hs1, S.len_dist);
   }
 }
 
-/* phase 4: canonical codes of both alphabets */
+/* phase 4: canonical codes of both alphabets, and where each alphabet's
+ * nonzero lengths end */
 PNG_HD void phase_codes(SegShared &S, int tid) {
-  canonical_codes(S.len_lit, NLIT, S.code_lit, tid, NT);
-  canonical_codes(S.len_dist, NDIST, S.code_dist, tid, NT);
+  for (int i = tid; i < OUT_BYTES / 4; i += NT) S.out[i] = 0; /* the sort keys are dead */
+  canonical_codes(S.len_lit, NLIT, S.hs0.first, S.code_lit, tid, NT);
+  canonical_codes(S.len_dist, NDIST, S.hs1.first, S.code_dist, tid, NT);
+  for (int i = tid; i < NLIT; i += NT)
+    if (S.len_lit[i]) atomic_max_u32(&S.lit_end, (uint32_t)i + 1);
+  for (int i = tid; i < NDIST; i += NT)
+    if (S.len_dist[i]) atomic_max_u32(&S.dist_end, (uint32_t)i + 1);
 }
 
-/* phase 5 (thread 0): run-length coded code lengths, the code-length code
- * and the header size */
-PNG_HD void phase_header(SegShared &S, int tid) {
-  if (tid != 0) return;
-  int hlit = NLIT;
-  while (hlit > 257 && S.len_lit[hlit - 1] == 0) hlit--;
-  int hdist = NDIST;
-  while (hdist > 1 && S.len_dist[hdist - 1] == 0) hdist--;
-  S.hlit = hlit;
-  S.hdist = hdist;
-  const int total = hlit + hdist;
-  auto L = [&](int i) -> int { return i < hlit ? S.len_lit[i] : S.len_dist[i - hlit]; };
-  int ncl = 0;
-  int i = 0;
-  while (i < total) {
-    const int v = L(i);
-    int run = 1;
-    while (i + run < total && L(i + run) == v) run++;
-    if (v == 0) {
-      int r = run;
-      while (r >= 11) {
-        const int c = r < 138 ? r : 138;
-        S.cl_sym[ncl] = 18, S.cl_extra[ncl++] = (uint8_t)(c - 11);
-        r -= c;
-      }
-      if (r >= 3) {
-        S.cl_sym[ncl] = 17, S.cl_extra[ncl++] = (uint8_t)(r - 3);
-        r = 0;
-      }
-      while (r > 0) S.cl_sym[ncl] = 0, S.cl_extra[ncl++] = 0, r--;
-    } else {
-      S.cl_sym[ncl] = (uint8_t)v, S.cl_extra[ncl++] = 0;
-      int r = run - 1;
-      while (r >= 3) {
-        const int c = r < 6 ? r : 6;
-        S.cl_sym[ncl] = 16, S.cl_extra[ncl++] = (uint8_t)(c - 3);
-        r -= c;
-      }
-      while (r > 0) S.cl_sym[ncl] = (uint8_t)v, S.cl_extra[ncl++] = 0, r--;
+/* The header's code lengths (RFC 1951 3.2.7): literal/length lengths
+ * 0..hlit-1 then distance lengths 0..hdist-1 as one sequence, run-length
+ * coded (16: repeat the previous length 3-6 times, 17: 3-10 zeros, 18:
+ * 11-138 zeros).  Done per run in parallel: each run start counts its
+ * entries, a scan places them, each run writes its own. */
+PNG_HD int hdr_len(const SegShared &S, int i) { return i < S.hlit ? S.len_lit[i] : S.len_dist[i - S.hlit]; }
+
+/* entries of the run of `run` copies of v (written at cl + off when cl) */
+PNG_HD int rle_run(int v, int run, uint8_t *sym, uint8_t *extra) {
+  int n = 0;
+  auto put = [&](int s_, int e_) {
+    if (sym) sym[n] = (uint8_t)s_, extra[n] = (uint8_t)e_;
+    n++;
+  };
+  if (v == 0) {
+    int r = run;
+    while (r >= 11) {
+      const int c = r < 138 ? r : 138;
+      put(18, c - 11);
+      r -= c;
     }
-    i += run;
+    if (r >= 3) {
+      put(17, r - 3);
+      r = 0;
+    }
+    while (r > 0) put(0, 0), r--;
+  } else {
+    put(v, 0);
+    int r = run - 1;
+    while (r >= 3) {
+      const int c = r < 6 ? r : 6;
+      put(16, c - 3);
+      r -= c;
+    }
+    while (r > 0) put(v, 0), r--;
   }
-  S.ncl = ncl;
-  for (int k = 0; k < ncl; k++) S.hist_cl[S.cl_sym[k]]++;
+  return n;
+}
+
+PNG_HD int run_at(const SegShared &S, int i, int total) {
+  const int v = hdr_len(S, i);
+  int run = 1;
+  while (i + run < total && hdr_len(S, i + run) == v) run++;
+  return run;
+}
+
+PNG_HD bool run_start(const SegShared &S, int i) { return i == 0 || hdr_len(S, i) != hdr_len(S, i - 1); }
+
+/* phase 5a: sizes, and each thread's count of entries over its indices */
+PNG_HD void phase_rle_count(SegShared &S, int tid) {
+  const int hlit = S.lit_end > 257 ? (int)S.lit_end : 257;
+  const int hdist = S.dist_end > 1 ? (int)S.dist_end : 1;
+  const int total = hlit + hdist;
+  if (tid == 0) S.hlit = hlit, S.hdist = hdist;
+  const int ch = (total + NT - 1) / NT;
+  int c = 0;
+  /* S.hlit is not yet visible to other threads: index with the local sizes */
+  for (int i = tid * ch; i < (tid + 1) * ch && i < total; i++) {
+    auto L = [&](int k) -> int { return k < hlit ? S.len_lit[k] : S.len_dist[k - hlit]; };
+    if (i == 0 || L(i) != L(i - 1)) {
+      int run = 1;
+      while (i + run < total && L(i + run) == L(i)) run++;
+      c += rle_run(L(i), run, nullptr, nullptr);
+    }
+  }
+  S.tbits[tid] = (uint32_t)c;
+}
+
+/* phase 5b (thread 0): offsets of the threads' entries */
+PNG_HD void phase_rle_scan(SegShared &S, int tid) {
+  if (tid != 0) return;
+  uint32_t off = 0;
+  for (int t = 0; t < NT; t++) {
+    const uint32_t c = S.tbits[t];
+    S.tbits[t] = off;
+    off += c;
+  }
+  S.ncl = (int)off;
+}
+
+/* phase 5c: the entries, and their code-length histogram */
+PNG_HD void phase_rle_write(SegShared &S, int tid) {
+  const int total = S.hlit + S.hdist;
+  const int ch = (total + NT - 1) / NT;
+  int off = (int)S.tbits[tid];
+  for (int i = tid * ch; i < (tid + 1) * ch && i < total; i++)
+    if (run_start(S, i)) {
+      const int n = rle_run(hdr_len(S, i), run_at(S, i, total), S.cl_sym + off, S.cl_extra + off);
+      for (int k = 0; k < n; k++) atomic_add_u32(&S.hist_cl[S.cl_sym[off + k]], 1);
+      off += n;
+    }
+}
+
+/* phase 5d (thread 0): the code-length code (19 symbols, max 7 bits) */
+PNG_HD void phase_cl_code(SegShared &S, int tid) {
+  if (tid != 0) return;
+  HuffScratchSmall &h = S.hs1;
   /* a code-length code must be complete: give a lone symbol a partner */
-  int used = count_used(S.hist_cl, NCL);
   uint32_t f2[NCL];
-  for (int k = 0; k < NCL; k++) f2[k] = S.hist_cl[k];
+  int used = 0;
+  for (int k = 0; k < NCL; k++) f2[k] = S.hist_cl[k], used += f2[k] ? 1 : 0;
   if (used < 2)
     for (int k = 0; k < NCL && used < 2; k++)
       if (!f2[k]) f2[k] = 1, used++;
-  /* 19 symbols: an insertion sort is enough */
-  HuffScratch &h = S.hs[1];
   int m = 0;
   for (int k = 0; k < NCL; k++) {
     if (!f2[k]) continue;
     int q = m++;
-    while (q > 0 && (f2[h.sorted[q - 1]] > f2[k])) {
+    while (q > 0 && h.wl[q - 1] > f2[k]) {
       h.sorted[q] = h.sorted[q - 1];
+      h.wl[q] = h.wl[q - 1];
       q--;
     }
     h.sorted[q] = (uint16_t)k;
+    h.wl[q] = f2[k];
   }
-  huff_lengths(f2, NCL, 7, h, S.len_cl);
-  canonical_codes(S.len_cl, NCL, S.code_cl, 0, 1);
+  h.nused = (uint32_t)m;
+  huff_lengths(7, h, S.len_cl);
+  canonical_codes(S.len_cl, NCL, h.first, S.code_cl, 0, 1);
   int hclen = NCL;
   while (hclen > 4 && S.len_cl[cl_order(hclen - 1)] == 0) hclen--;
   S.hclen = hclen;
-  uint32_t bits = 3 + 5 + 5 + 4 + 3 * hclen;
-  for (int k = 0; k < ncl; k++) {
+  S.hdr_bits = 3 + 5 + 5 + 4 + 3 * hclen;
+}
+
+/* phase 5e: the header's size */
+PNG_HD void phase_hdr_bits(SegShared &S, int tid) {
+  uint32_t bits = 0;
+  for (int k = tid; k < S.ncl; k += NT) {
     const int s = S.cl_sym[k];
     bits += S.len_cl[s] + (s == 16 ? 2 : s == 17 ? 3 : s == 18 ? 7 : 0);
   }
-  S.hdr_bits = bits;
+  if (bits) atomic_add_u32(&S.hdr_bits, bits);
 }
 
 /* phase 6: bits of each thread's tokens */
 PNG_HD void phase_count(SegShared &S, const SegArgs &A, int seg, int tid) {
   long long b, e;
   sub_range(A, seg, tid, b, e);
+  (void)b, (void)e;
   CountSink cs{&S, 0};
-  parse(A.F, b, e, S.dist, S.nd, cs);
+  replay(thread_tokens(A, seg, tid), S.ntok[tid], cs);
   S.tbits[tid] = cs.bits;
 }
 
@@ -600,7 +940,7 @@ PNG_HD void phase_emit(SegShared &S, const SegArgs &A, int seg, int tid) {
     /* bytes 5.. by whole words where each thread owns them */
     for (uint32_t i = (uint32_t)tid; i < n; i += NT) {
       const uint32_t pos = 5 + i;
-      atomic_or_u32(&S.out[pos >> 2], (uint32_t)A.F[sb + i] << (8 * (pos & 3)));
+      atomic_or_u32(&S.out[pos >> 2], (uint32_t)S.win[sb - S.w0 + i] << (8 * (pos & 3)));
     }
     return;
   }
@@ -638,7 +978,8 @@ PNG_HD void phase_emit(SegShared &S, const SegArgs &A, int seg, int tid) {
   sub_range(A, seg, tid, b, e);
   EmitSink es{&S, {}};
   es.w.start(S.out, S.tbits[tid]);
-  parse(A.F, b, e, S.dist, S.nd, es);
+  (void)b, (void)e;
+  replay(thread_tokens(A, seg, tid), S.ntok[tid], es);
   es.w.flush();
 }
 
@@ -676,13 +1017,13 @@ PNG_HD void phase_store(SegShared &S, const SegArgs &A, int seg, int tid) {
   for (uint32_t i = (uint32_t)tid; i < nw; i += NT) dst[i] = S.out[i];
   if (tid == 0) {
     const uint32_t n = 4 + S.nbytes;
-    const uint32_t crc = gf2_mult(0xFFFFFFFFu, gf2_xpow(8ull * n)) ^ S.crc_part[0] ^ 0xFFFFFFFFu;
+    (void)n;
+    const uint32_t crc = gf2_mult(0xFFFFFFFFu, S.crc_xn) ^ S.crc_part[0] ^ 0xFFFFFFFFu;
     unsigned long long s1 = 0, s2 = 0, after = 0;
     for (int t = NT - 1; t >= 0; t--) {
       s1 += S.a1[t];
       s2 += S.a2[t] + (unsigned long long)S.a1[t] * after;
       after += S.alen[t];
-      s2 %= ADLER_MOD;
     }
     SegMeta m;
     m.nbytes = S.nbytes;
