@@ -162,6 +162,23 @@ def cpu_baseline(steps=1, quality=CPU_QUALITY):
                       f"{quality / 10:g} ({st1.num_iters / 1e6:.0f} M iterations)"}, times
 
 
+def png_cpu_baseline(img, steps=3):
+    """write_png's CPU path on the same image: the oracle's restatement of
+    libpng's row filtering, then zlib at libpng's default level (6), one
+    thread as libpng runs.  Returns (median seconds, zlib bytes)."""
+    import zlib
+
+    import _oracle
+
+    times, n = [], 0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        F = _oracle.png_filter(img, fast=True)
+        n = len(zlib.compress(F.tobytes(), 6))
+        times.append(time.perf_counter() - t0)
+    return statistics.median(times), n
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -500,6 +517,50 @@ def run_legs(args):
         out["batched_mixed"] = leg_batched("mixed", jobs, "mixed: %d jobs" % args.mixed_jobs)
     if "served" in legs:
         out["served"] = leg_served(args.served_requests)
+    if "png" in legs:
+        out["png"] = leg_png(args)
+    return out
+
+
+def leg_png(args, steps=10, warm=3):
+    """write_png (png.c:36) on the device: the still render's RGBA8 image
+    (as flam3-render writes PNGs, 4 channels) encoded through
+    flam3gpu_encode_png from host memory, and flam3gpu_render_png (render
+    and encode with the pixels kept on the device), against the CPU path
+    write_png runs (row filters + zlib level 6, one thread)."""
+    from flam3_gb300 import genome as gm, render
+
+    G = gm.still_genome(1)
+    img, _ = render.render(gm.Frame(G, bits=33, seed="png"), nchan=4)
+    e2e, kern = [], []
+    png = b""
+    for i in range(warm + steps):
+        t0 = time.perf_counter()
+        png = render.encode_png(img)
+        dt = time.perf_counter() - t0
+        if i >= warm:
+            e2e.append(dt)
+            kern.append(render.png_last_ms())
+    fused, plain = [], []
+    for i in range(2 + 3):
+        t0 = time.perf_counter()
+        render.render_png(gm.Frame(G, bits=33, seed="png-%d" % i))
+        t1 = time.perf_counter()
+        render.render(gm.Frame(G, bits=33, seed="png-%d" % i), nchan=4)
+        t2 = time.perf_counter()
+        if i >= 2:
+            fused.append(t1 - t0)
+            plain.append(t2 - t1)
+    k = statistics.median(kern)
+    out = {"image": "%dx%d RGBA8 (the still workload's render)" % (img.shape[1], img.shape[0]),
+           "raw_bytes": int(img.nbytes), "png_bytes": len(png),
+           "encode_kernel_ms": k, "encode_gbps": img.nbytes / (k * 1e-3) / 1e9,
+           "encode_e2e_ms": 1e3 * statistics.median(e2e),
+           "render_png_ms": 1e3 * statistics.median(fused), "render_only_ms": 1e3 * statistics.median(plain)}
+    if not args.no_cpu:
+        cpu_s, zbytes = png_cpu_baseline(img)
+        out["cpu_baseline"] = {"encode_ms": 1e3 * cpu_s, "zlib6_bytes": zbytes, "cores": 1, "kind": "port",
+                               "sample": "oracle row filters + zlib.compress level 6 on the same image"}
     return out
 
 
@@ -510,8 +571,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--legs", default="animation,mixed,served",
-                    help="batched/served legs to add (animation,mixed,served; empty: none)")
+    ap.add_argument("--legs", default="animation,mixed,served,png",
+                    help="batched/served/PNG legs to add (animation,mixed,served,png; empty: none)")
     ap.add_argument("--animation-frames", type=int, default=120)
     ap.add_argument("--mixed-jobs", type=int, default=256)
     ap.add_argument("--served-requests", type=int, default=64)
