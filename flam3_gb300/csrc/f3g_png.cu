@@ -17,8 +17,33 @@ namespace {
 
 constexpr int FT = 256; /* threads of the filter kernel */
 
+/* the filtered bytes of 4 consecutive stream bytes (x, left a, up b,
+ * up-left c as little-endian words) for filter k */
+__device__ __forceinline__ uint32_t filter_word(int k, uint32_t x, uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t o = 0;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int sh = 8 * q;
+    o |= (uint32_t)filter_byte(k, (x >> sh) & 255, (a >> sh) & 255, (b >> sh) & 255, (c >> sh) & 255) << sh;
+  }
+  return o;
+}
+
+__device__ __forceinline__ uint32_t cost_word(int k, uint32_t x, uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t s = 0;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int sh = 8 * q;
+    s += filter_cost(filter_byte(k, (x >> sh) & 255, (a >> sh) & 255, (b >> sh) & 255, (c >> sh) & 255));
+  }
+  return s;
+}
+
 /* row r of the image, in PNG byte order (16-bit samples big-endian: the
- * image holds them little-endian, as png_set_swap undoes in png.c:105-107) */
+ * image holds them little-endian, as png_set_swap undoes in png.c:105-107).
+ * RGBA rows (4 or 8 bytes per pixel) are read as words: the left neighbour
+ * is the previous word (8-bit) or the one before (16-bit, bytes of each
+ * sample swapped with a byte permute); RGB rows byte by byte. */
 __global__ void __launch_bounds__(FT) k_png_filter(const uint8_t *__restrict__ img, int w, int h, int bpp, int bpc,
                                                    uint8_t *__restrict__ F) {
   const int r = blockIdx.x;
@@ -26,14 +51,36 @@ __global__ void __launch_bounds__(FT) k_png_filter(const uint8_t *__restrict__ i
   const uint8_t *row = img + (long long)r * RB;
   const uint8_t *up = r ? row - RB : nullptr;
   const int sw = bpc == 2 ? 1 : 0;
+  /* word path: 4-byte aligned rows of whole words with a whole-word left
+   * neighbour */
+  const bool words = (bpp == 4 || bpp == 8) && ((reinterpret_cast<uintptr_t>(img) & 3) == 0);
+  const int lw = bpp / 4; /* left neighbour distance in words */
+  const uint32_t *row4 = reinterpret_cast<const uint32_t *>(row);
+  const uint32_t *up4 = reinterpret_cast<const uint32_t *>(up);
+  const long long nw = RB / 4;
+  auto ld = [&](const uint32_t *p, long long i) -> uint32_t {
+    const uint32_t v = p[i];
+    return sw ? __byte_perm(v, 0, 0x2301) : v;
+  };
   uint32_t s[5] = {0, 0, 0, 0, 0};
-  for (long long i = threadIdx.x; i < RB; i += FT) {
-    const int x = row[i ^ sw];
-    const int a = i >= bpp ? row[(i - bpp) ^ sw] : 0;
-    const int b = up ? up[i ^ sw] : 0;
-    const int c = (up && i >= bpp) ? up[(i - bpp) ^ sw] : 0;
+  if (words) {
+    for (long long i = threadIdx.x; i < nw; i += FT) {
+      const uint32_t x = ld(row4, i);
+      const uint32_t a = i >= lw ? ld(row4, i - lw) : 0;
+      const uint32_t b = up ? ld(up4, i) : 0;
+      const uint32_t c = (up && i >= lw) ? ld(up4, i - lw) : 0;
 #pragma unroll
-    for (int k = 0; k < 5; k++) s[k] += filter_cost(filter_byte(k, x, a, b, c));
+      for (int k = 0; k < 5; k++) s[k] += cost_word(k, x, a, b, c);
+    }
+  } else {
+    for (long long i = threadIdx.x; i < RB; i += FT) {
+      const int x = row[i ^ sw];
+      const int a = i >= bpp ? row[(i - bpp) ^ sw] : 0;
+      const int b = up ? up[i ^ sw] : 0;
+      const int c = (up && i >= bpp) ? up[(i - bpp) ^ sw] : 0;
+#pragma unroll
+      for (int k = 0; k < 5; k++) s[k] += filter_cost(filter_byte(k, x, a, b, c));
+    }
   }
   __shared__ uint32_t red[5][FT / 32];
   __shared__ int best;
@@ -59,12 +106,24 @@ __global__ void __launch_bounds__(FT) k_png_filter(const uint8_t *__restrict__ i
   const int k = best;
   uint8_t *o = F + (long long)r * (RB + 1);
   if (threadIdx.x == 0) o[0] = (uint8_t)k;
-  for (long long i = threadIdx.x; i < RB; i += FT) {
-    const int x = row[i ^ sw];
-    const int a = i >= bpp ? row[(i - bpp) ^ sw] : 0;
-    const int b = up ? up[i ^ sw] : 0;
-    const int c = (up && i >= bpp) ? up[(i - bpp) ^ sw] : 0;
-    o[1 + i] = (uint8_t)filter_byte(k, x, a, b, c);
+  if (words) {
+    for (long long i = threadIdx.x; i < nw; i += FT) {
+      const uint32_t x = ld(row4, i);
+      const uint32_t a = i >= lw ? ld(row4, i - lw) : 0;
+      const uint32_t b = up ? ld(up4, i) : 0;
+      const uint32_t c = (up && i >= lw) ? ld(up4, i - lw) : 0;
+      const uint32_t v = filter_word(k, x, a, b, c);
+      uint8_t *d = o + 1 + 4 * i; /* 1 + 4i: not word aligned */
+      d[0] = (uint8_t)v, d[1] = (uint8_t)(v >> 8), d[2] = (uint8_t)(v >> 16), d[3] = (uint8_t)(v >> 24);
+    }
+  } else {
+    for (long long i = threadIdx.x; i < RB; i += FT) {
+      const int x = row[i ^ sw];
+      const int a = i >= bpp ? row[(i - bpp) ^ sw] : 0;
+      const int b = up ? up[i ^ sw] : 0;
+      const int c = (up && i >= bpp) ? up[(i - bpp) ^ sw] : 0;
+      o[1 + i] = (uint8_t)filter_byte(k, x, a, b, c);
+    }
   }
 }
 
