@@ -308,13 +308,9 @@ int f3g_png_encode_idat(const void *d_img, int w, int h, int nchan, int bpc, voi
   uint8_t *stage = F + ((fb + 255) / 256) * 256;
   SegMeta *meta = (SegMeta *)(stage + (size_t)ns * STAGE);
   uint16_t *tokens = (uint16_t *)(meta + ns);
-  static int attr_set = 0;
   const int smem = (int)sizeof(SegShared);
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(k_png_deflate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-      return 2;
-    attr_set = 1;
-  }
+  /* per device and cheap: set on every call */
+  if (cudaFuncSetAttribute(k_png_deflate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 2;
   k_png_filter<<<h, FT, 0, st>>>((const uint8_t *)d_img, w, h, bpp, bpc, F);
   SegArgs A;
   A.F = F;

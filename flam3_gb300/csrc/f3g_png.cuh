@@ -6,15 +6,18 @@
  * one zlib stream split over IDAT chunks.
  *
  * Here the filtered stream (h rows of 1 + w*bpp bytes) is cut into
- * segments of PNG_SEG bytes and each segment is deflated by one CTA on its
- * own: a greedy LZ77 parse over a few candidate distances that suit images
- * (1, one pixel, two pixels, one row), one dynamic-Huffman block per
- * segment (a stored block where that is smaller), the segment ended on a
- * byte boundary by an empty stored block, so every segment becomes one IDAT
- * chunk whose CRC the CTA computes itself.  Back-references may reach into
- * earlier segments (the decoder holds all of the stream), so cutting costs
- * only the few bytes of each block header.  The zlib header and the Adler-32
- * trailer are two small IDAT chunks of their own.
+ * segments of SEG (16 KB) bytes and each segment is deflated by one CTA on
+ * its own.  The segment and the LOOKBACK bytes before it are staged in
+ * shared memory; each thread parses SUB bytes greedily against fixed
+ * distances that suit images (neighbouring pixels, the row above and its
+ * diagonals, two rows) and a table of the latest 4-byte occurrences in the
+ * look-back; the segment becomes one dynamic-Huffman block (a stored block
+ * where that is smaller), ended on a byte boundary by an empty stored block,
+ * so every segment is one IDAT chunk whose CRC the CTA computes itself.
+ * Back-references may reach into earlier segments (the decoder holds all of
+ * the stream), so cutting costs only the few bytes of each block header.
+ * The zlib header and the Adler-32 trailer are two small IDAT chunks of
+ * their own.
  *
  * Format constants follow RFC 1950 (zlib), RFC 1951 (deflate) and the PNG
  * specification (chunk layout, CRC-32 polynomial, filter types).
