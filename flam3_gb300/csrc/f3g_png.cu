@@ -135,7 +135,9 @@ __global__ void __launch_bounds__(NT) k_png_deflate(SegArgs A) {
   __syncthreads();
   phase_window(S, A, seg, tid);
   __syncthreads();
-  phase_hist(S, A, seg, tid);
+  phase_parse(S, A, seg, tid);
+  __syncthreads();
+  phase_trim(S, A, seg, tid);
   __syncthreads();
   phase_keys(S, tid);
   __syncthreads();
@@ -286,7 +288,7 @@ size_t f3g_png_work_bytes(int w, int h, int nchan, int bpc) {
   const long long fb = f3g_png_filtered_bytes(w, h, nchan, bpc);
   const long long ns = f3g_png_segments(w, h, nchan, bpc);
   return (size_t)(((fb + 255) / 256) * 256 + ns * STAGE + ns * (long long)sizeof(SegMeta) +
-                  ns * (long long)SEG * 2);
+                  ns * (long long)TOK_PER_SEG * 2);
 }
 
 /* the IDAT chunks' bytes, at most */

@@ -42,6 +42,7 @@ constexpr int NT = 256;             /* threads per CTA */
 constexpr int LOG_NT = 8;
 constexpr int SUB = SEG / NT;       /* bytes parsed by one thread */
 constexpr int MIN_MATCH = 4;        /* shortest match emitted (3 is legal) */
+constexpr int OVERRUN = 64;         /* how far a thread's last match may run past its share */
 constexpr int MAX_MATCH = 258;
 constexpr int WINDOW = 32768;       /* deflate's largest distance */
 constexpr int LOOKBACK = 16384;     /* bytes before a segment that its matches may reach */
@@ -212,16 +213,17 @@ PNG_HD int best_match(const uint8_t *F, long long p, long long end, const Cands 
   return bl;
 }
 
-/* Greedy parse of F[beg, end): the longest candidate match at each
- * position when it is at least MIN_MATCH long, else a literal.  (One step of
- * lazy evaluation, as zlib does, gains under 1 % on rendered images for
- * twice the search.) */
+/* Greedy parse from beg while the position is before end: the longest
+ * candidate match at each position (it may run on up to `limit`, past end)
+ * when it is at least MIN_MATCH long, else a literal.  Returns the position
+ * after the last token.  (One step of lazy evaluation, as zlib does, gains
+ * under 1 % on rendered images for twice the search.) */
 template <class Sink>
-PNG_HD void parse(const uint8_t *F, long long beg, long long end, const Cands &C, Sink &s) {
+PNG_HD long long parse(const uint8_t *F, long long beg, long long end, long long limit, const Cands &C, Sink &s) {
   long long p = beg;
   while (p < end) {
     int bd;
-    const int bl = best_match(F, p, end, C, bd);
+    const int bl = best_match(F, p, limit, C, bd);
     if (bl >= MIN_MATCH) {
       s.match(bl, bd);
       p += bl;
@@ -230,6 +232,7 @@ PNG_HD void parse(const uint8_t *F, long long beg, long long end, const Cands &C
       p++;
     }
   }
+  return p;
 }
 
 /* ---- shared state of one segment's CTA ---- */
@@ -265,6 +268,8 @@ struct SegShared {
     uint32_t crc_part[NT];      /* per-thread CRC registers, after the block is out */
   };
   int ntok[NT];                 /* per-thread token entries */
+  int tend[NT];                 /* where each thread's last token ends (relative to w0) */
+  uint16_t tstart[NT], tfrom[NT]; /* a thread's first byte, its first uncovered byte */
   uint32_t crc_x[8];            /* x^(8 q 2^l) mod the CRC polynomial */
   uint32_t crc_xn;              /* x^(8 n), n = 4 + the segment's bytes */
   uint32_t a1[NT], a2[NT], alen[NT]; /* Adler-32 partial sums per thread */
@@ -282,22 +287,66 @@ struct SegShared {
 
 /* ---- sinks of the parse ---- */
 
-struct HistSink {
-  SegShared *S;
+/* records a thread's tokens */
+struct TokSink {
   uint16_t *tok;
   int n;
-  PNG_HD void literal(uint8_t v) {
-    atomic_add_u32(&S->hist_lit[v], 1);
-    tok[(size_t)(n++) * NT] = v;
+  PNG_HD void literal(uint8_t v) { tok[(size_t)(n++) * NT] = v; }
+  PNG_HD void match(int L, int d) {
+    tok[(size_t)(n++) * NT] = (uint16_t)(256 + L - 3);
+    tok[(size_t)(n++) * NT] = (uint16_t)(d - 1);
   }
+};
+
+/* adds (or, with inc = 0xFFFFFFFF, removes) tokens' symbols in the histograms */
+struct HistSink {
+  SegShared *S;
+  uint32_t inc;
+  PNG_HD void literal(uint8_t v) { atomic_add_u32(&S->hist_lit[v], inc); }
   PNG_HD void match(int L, int d) {
     int s, nx, e;
     len_code(L, s, nx, e);
-    atomic_add_u32(&S->hist_lit[s], 1);
+    atomic_add_u32(&S->hist_lit[s], inc);
     dist_code(d, s, nx, e);
-    atomic_add_u32(&S->hist_dist[s], 1);
-    tok[(size_t)(n++) * NT] = (uint16_t)(256 + L - 3);
-    tok[(size_t)(n++) * NT] = (uint16_t)(d - 1);
+    atomic_add_u32(&S->hist_dist[s], inc);
+  }
+};
+
+/* records a thread's tokens and counts their symbols */
+struct ParseSink {
+  TokSink t;
+  HistSink h;
+  PNG_HD void literal(uint8_t v) { t.literal(v), h.literal(v); }
+  PNG_HD void match(int L, int d) { t.match(L, d), h.match(L, d); }
+};
+
+/* A thread's final match may run past its share; the bytes it covers are
+ * dropped from the following threads' tokens: tokens that end at or before
+ * `from` are skipped, a match that straddles it keeps its tail (the same
+ * distance still matches there) or, when that is under 3 bytes, turns into
+ * literals. */
+template <class Sink>
+struct TrimSink {
+  Sink &inner;
+  const uint8_t *F;
+  long long pos, from;
+  PNG_HD void literal(uint8_t v) {
+    if (pos >= from) inner.literal(v);
+    pos++;
+  }
+  PNG_HD void match(int L, int d) {
+    const long long e = pos + L;
+    if (pos >= from) {
+      inner.match(L, d);
+    } else if (e > from) {
+      const int k = (int)(e - from);
+      if (k >= 3) {
+        inner.match(k, d);
+      } else {
+        for (long long q = from; q < e; q++) inner.literal(F[q]);
+      }
+    }
+    pos = e;
   }
 };
 
@@ -566,13 +615,19 @@ struct SegArgs {
   int nseg;
   uint8_t *stage;     /* nseg x STAGE bytes */
   SegMeta *meta;
-  uint16_t *tokens;   /* nseg x SEG parse tokens, interleaved over the threads */
+  uint16_t *tokens;   /* nseg x TOK_PER_SEG parse tokens, interleaved over the threads */
 };
 
 /* A thread's parse tokens: a literal is one entry (the byte), a match two
- * (256 + length - 3, then distance - 1); never more entries than bytes.
- * Entry k of thread t sits at k * NT + t of the segment's area. */
-PNG_HD uint16_t *thread_tokens(const SegArgs &A, int seg, int tid) { return A.tokens + (size_t)seg * SEG + tid; }
+ * (256 + length - 3, then distance - 1).  A match takes at least 4 bytes,
+ * but the thread's last one may start at its last byte, so a thread records
+ * at most SUB + 1 entries.  Entry k of thread t sits at k * NT + t of the
+ * segment's area of TOK_PER_SEG entries. */
+constexpr int TOK_PER_THREAD = SUB + 2;
+constexpr int TOK_PER_SEG = TOK_PER_THREAD * NT;
+PNG_HD uint16_t *thread_tokens(const SegArgs &A, int seg, int tid) {
+  return A.tokens + (size_t)seg * TOK_PER_SEG + tid;
+}
 
 PNG_HD void seg_range(const SegArgs &A, int seg, long long &b, long long &e) {
   b = (long long)seg * SEG;
@@ -650,14 +705,16 @@ PNG_HD void phase_window(SegShared &S, const SegArgs &A, int seg, int tid) {
   }
 }
 
-/* phase 1: symbol histogram and Adler-32 partial sums */
-PNG_HD void phase_hist(SegShared &S, const SegArgs &A, int seg, int tid) {
+/* phase 1: the parse (tokens, where the thread's last token ends) and the
+ * Adler-32 partial sums */
+PNG_HD void phase_parse(SegShared &S, const SegArgs &A, int seg, int tid) {
   long long b, e;
   sub_range(A, seg, tid, b, e);
-  HistSink hsink{&S, thread_tokens(A, seg, tid), 0};
+  ParseSink ps{{thread_tokens(A, seg, tid), 0}, {&S, 1u}};
   const long long rb = b - S.w0, re = e - S.w0;
-  parse(S.win, rb, re, S.cands(), hsink);
-  S.ntok[tid] = hsink.n;
+  const long long lim = re + OVERRUN < (long long)S.wlen ? re + OVERRUN : (long long)S.wlen;
+  S.tend[tid] = (int)parse(S.win, rb, re, lim, S.cands(), ps);
+  S.ntok[tid] = ps.t.n;
   unsigned long long s1 = 0, s2 = 0;
   for (long long p = rb; p < re; p++) {
     s1 += S.win[p];
@@ -666,7 +723,49 @@ PNG_HD void phase_hist(SegShared &S, const SegArgs &A, int seg, int tid) {
   S.a1[tid] = (uint32_t)s1;
   S.a2[tid] = (uint32_t)s2;
   S.alen[tid] = (uint32_t)(e - b);
+}
+
+/* replays thread tid's tokens, trimmed to the bytes no earlier thread's
+ * final match covers (matches are at most 258 bytes, so only the five
+ * threads before can reach into this share) */
+template <class Sink>
+PNG_HD void replay_trimmed(const SegShared &S, const SegArgs &A, int seg, int tid, Sink &s) {
+  TrimSink<Sink> t{s, S.win, (long long)S.tstart[tid], (long long)S.tfrom[tid]};
+  replay(thread_tokens(A, seg, tid), S.ntok[tid], t);
+}
+
+/* phase 1b: each thread's first uncovered byte; the histogram loses the
+ * symbols of the tokens (or token heads) that byte drops and gains their
+ * replacements -- only the thread's first few tokens are walked */
+PNG_HD void phase_trim(SegShared &S, const SegArgs &A, int seg, int tid) {
+  long long b, e;
+  sub_range(A, seg, tid, b, e);
+  (void)e;
+  const int start = (int)(b - S.w0);
+  int from = start;
+  for (int j = tid - 1; j >= 0 && j >= tid - 5; j--) from = S.tend[j] > from ? S.tend[j] : from;
+  S.tstart[tid] = start;
+  S.tfrom[tid] = from;
   if (tid == 0) atomic_add_u32(&S.hist_lit[256], 1); /* end of block */
+  if (from == start) return;
+  HistSink sub{&S, 0xFFFFFFFFu}, add{&S, 1u};
+  TrimSink<HistSink> keep{add, S.win, (long long)start, (long long)from};
+  const uint16_t *tok = thread_tokens(A, seg, tid);
+  long long pos = start;
+  for (int i = 0; i < S.ntok[tid] && pos < from; i++) {
+    const int v = tok[(size_t)i * NT];
+    if (v < 256) {
+      sub.literal((uint8_t)v);
+      keep.literal((uint8_t)v);
+      pos++;
+    } else {
+      const int L = v - 253, d = tok[(size_t)(i + 1) * NT] + 1;
+      sub.match(L, d);
+      keep.match(L, d);
+      pos += L;
+      i++;
+    }
+  }
 }
 
 /* phase 2a: sort keys of both alphabets' symbols, (alphabet, frequency,
@@ -895,7 +994,7 @@ PNG_HD void phase_count(SegShared &S, const SegArgs &A, int seg, int tid) {
   sub_range(A, seg, tid, b, e);
   (void)b, (void)e;
   CountSink cs{&S, 0};
-  replay(thread_tokens(A, seg, tid), S.ntok[tid], cs);
+  replay_trimmed(S, A, seg, tid, cs);
   S.tbits[tid] = cs.bits;
 }
 
@@ -982,7 +1081,7 @@ PNG_HD void phase_emit(SegShared &S, const SegArgs &A, int seg, int tid) {
   EmitSink es{&S, {}};
   es.w.start(S.out, S.tbits[tid]);
   (void)b, (void)e;
-  replay(thread_tokens(A, seg, tid), S.ntok[tid], es);
+  replay_trimmed(S, A, seg, tid, es);
   es.w.flush();
 }
 
