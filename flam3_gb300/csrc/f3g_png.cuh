@@ -439,12 +439,6 @@ struct EmitSink {
 
 /* rank of symbol `sym` among the used symbols by (frequency, symbol); run
  * by every thread for its symbols, fills h.sorted */
-PNG_HD int count_used(const uint32_t *freq, int n) {
-  int m = 0;
-  for (int s = 0; s < n; s++) m += freq[s] ? 1 : 0;
-  return m;
-}
-
 /* Huffman code lengths limited to maxbits, forming a complete code (Kraft
  * sum exactly 1) whenever at least two symbols are used; one used symbol
  * gets length 1.  h.sorted / h.wl / h.nused hold the used symbols in
@@ -575,22 +569,9 @@ constexpr X8Table make_x8() {
 __constant__ X8Table c_x8 = make_x8();
 #endif
 
-/* x^(8 n) modulo the CRC polynomial, one thread */
-PNG_HD uint32_t xpow8(uint32_t n) {
-#ifdef __CUDA_ARCH__
-  const X8Table &t = c_x8;
-#else
-  static constexpr X8Table t = make_x8();
-#endif
-  uint32_t r = 0x80000000u;
-  for (int k = 0; k < 32; k++)
-    if ((n >> k) & 1u) r = gf2_mult(r, t.v[k]);
-  return r;
-}
-
 #ifdef __CUDACC__
-/* the same over a whole warp (every lane gets the product): lane k holds
- * the factor of bit k, then a butterfly of products */
+/* x^(8 n) modulo the CRC polynomial over a whole warp (every lane gets the
+ * product): lane k holds the factor of bit k, then a butterfly of products */
 __device__ __forceinline__ uint32_t xpow8_warp(uint32_t n) {
   const int lane = threadIdx.x & 31;
   uint32_t f = ((n >> lane) & 1u) ? c_x8.v[lane] : 0x80000000u;
