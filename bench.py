@@ -551,16 +551,36 @@ def leg_png(args, steps=10, warm=3):
         if i >= 2:
             fused.append(t1 - t0)
             plain.append(t2 - t1)
+    # animation frames written as PNG (flam3-animate's loop): render and
+    # encode on the device, against the raw render plus the CPU encode
+    nf = 24
+    gs = gm.animation_keys(2)
+    anim = lambda i: gm.Frame(gs, bits=33, seed="png-anim-%d" % i, time=float(i))
+    render.render_png(anim(0))
+    t0 = time.perf_counter()
+    for i in range(nf):
+        render.render_png(anim(i))
+    anim_png_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    last = None
+    for i in range(nf):
+        last, _ = render.render(anim(i), nchan=4)
+    anim_raw_s = time.perf_counter() - t0
     k = statistics.median(kern)
     out = {"image": "%dx%d RGBA8 (the still workload's render)" % (img.shape[1], img.shape[0]),
            "raw_bytes": int(img.nbytes), "png_bytes": len(png),
            "encode_kernel_ms": k, "encode_gbps": img.nbytes / (k * 1e-3) / 1e9,
            "encode_e2e_ms": 1e3 * statistics.median(e2e),
-           "render_png_ms": 1e3 * statistics.median(fused), "render_only_ms": 1e3 * statistics.median(plain)}
+           "render_png_ms": 1e3 * statistics.median(fused), "render_only_ms": 1e3 * statistics.median(plain),
+           "animation_png_fps": nf / anim_png_s, "animation_raw_fps": nf / anim_raw_s,
+           "animation": "%d frames of the animation workload (1280x720 q500, 100 temporal samples, DE7) through "
+                        "flam3gpu_render_png, against flam3gpu_render with raw RGBA out" % nf}
     if not args.no_cpu:
         cpu_s, zbytes = png_cpu_baseline(img)
         out["cpu_baseline"] = {"encode_ms": 1e3 * cpu_s, "zlib6_bytes": zbytes, "cores": 1, "kind": "port",
                                "sample": "oracle row filters + zlib.compress level 6 on the same image"}
+        frame_cpu_s, _ = png_cpu_baseline(last)
+        out["cpu_baseline"]["animation_fps_with_cpu_png"] = nf / (anim_raw_s + nf * frame_cpu_s)
     return out
 
 
