@@ -566,6 +566,11 @@ def leg_png(args, steps=10, warm=3):
     for i in range(nf):
         last, _ = render.render(anim(i), nchan=4)
     anim_raw_s = time.perf_counter() - t0
+    from flam3_gb300 import service
+    service.render_batch_png([anim(i) for i in range(2)])
+    t0 = time.perf_counter()
+    service.render_batch_png([anim(i) for i in range(nf)])
+    anim_batch_png_s = time.perf_counter() - t0
     k = statistics.median(kern)
     out = {"image": "%dx%d RGBA8 (the still workload's render)" % (img.shape[1], img.shape[0]),
            "raw_bytes": int(img.nbytes), "png_bytes": len(png),
@@ -573,8 +578,10 @@ def leg_png(args, steps=10, warm=3):
            "encode_e2e_ms": 1e3 * statistics.median(e2e),
            "render_png_ms": 1e3 * statistics.median(fused), "render_only_ms": 1e3 * statistics.median(plain),
            "animation_png_fps": nf / anim_png_s, "animation_raw_fps": nf / anim_raw_s,
+           "animation_batched_png_fps": nf / anim_batch_png_s,
            "animation": "%d frames of the animation workload (1280x720 q500, 100 temporal samples, DE7) through "
-                        "flam3gpu_render_png, against flam3gpu_render with raw RGBA out" % nf}
+                        "flam3gpu_render_png, against flam3gpu_render with raw RGBA out; batched: "
+                        "flam3gpu_render_batch_png" % nf}
     if not args.no_cpu:
         cpu_s, zbytes = png_cpu_baseline(img)
         out["cpu_baseline"] = {"encode_ms": 1e3 * cpu_s, "zlib6_bytes": zbytes, "cores": 1, "kind": "port",

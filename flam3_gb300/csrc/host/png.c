@@ -20,6 +20,7 @@
 #include "f3g_host.h"
 #include "f3g_launch.h"
 #include "flam3_gpu.h"
+#include "flam3_gpu_service.h"
 
 /* ---- chunk writing (host side, a few bytes) ---- */
 
@@ -344,3 +345,71 @@ int flam3gpu_png_last_ms(double *encode_ms) {
   return 0;
 }
 
+
+/* flam3-animate's frame loop with PNG output (flam3-animate.c:225-310):
+ * the frames render through a render service (all admitted together) and
+ * each is encoded on the device as soon as it completes, on this thread's
+ * stream while the service renders the rest. */
+int flam3gpu_render_batch_png(flam3_frame *frames, int n, int transp, stat_struct *stats, unsigned char **pngs,
+                              size_t *lens) {
+  f3g_clear_error();
+  if (n < 1) return 0;
+  if (!frames || !stats || !pngs || !lens) {
+    f3g_set_error("NULL argument");
+    return 1;
+  }
+  for (int i = 0; i < n; i++) pngs[i] = NULL, lens[i] = 0;
+  flam3gpu_service_config cfg;
+  flam3gpu_service_default_config(&cfg);
+  cfg.round_samples = -1;
+  void **outs = (void **)calloc((size_t)n, sizeof(void *));
+  uint64_t *tk = (uint64_t *)calloc((size_t)n, sizeof(uint64_t));
+  int rv = 0;
+  if (!outs || !tk) {
+    f3g_set_error("out of host memory");
+    free(outs);
+    free(tk);
+    return 1;
+  }
+  for (int i = 0; i < n && !rv; i++) {
+    const flam3_genome *g = &frames[i].genomes[0];
+    outs[i] = malloc((size_t)g->width * g->height * 4 * frames[i].bytes_per_channel);
+    if (!outs[i]) {
+      f3g_set_error("out of host memory");
+      rv = 1;
+    }
+  }
+  flam3gpu_service *s = rv ? NULL : flam3gpu_service_create(&cfg);
+  if (!rv && !s) rv = 1;
+  if (!rv) rv = flam3gpu_service_submit_many(s, frames, n, outs, flam3_field_both, 4, transp, tk);
+  char first_err[256] = "";
+  for (int i = 0; i < n && s; i++) {
+    if (!tk[i]) continue;
+    if (flam3gpu_service_wait(s, tk[i], -1, &stats[i], NULL)) {
+      if (!first_err[0]) snprintf(first_err, sizeof(first_err), "%s", flam3gpu_last_error());
+      rv = 1;
+      continue;
+    }
+    char badvals[64], numiters[64], rtime[32];
+    snprintf(badvals, sizeof(badvals), "%g", stats[i].badvals / (double)stats[i].num_iters);
+    snprintf(numiters, sizeof(numiters), "%g", (double)stats[i].num_iters);
+    snprintf(rtime, sizeof(rtime), "%d", stats[i].render_seconds);
+    flam3gpu_png_text t[8];
+    const int nt = comment_texts(NULL, badvals, numiters, rtime, t);
+    const flam3_genome *g = &frames[i].genomes[0];
+    if (flam3gpu_encode_png(outs[i], 0, g->width, g->height, 4, frames[i].bytes_per_channel, t, nt, &pngs[i],
+                            &lens[i])) {
+      if (!first_err[0]) snprintf(first_err, sizeof(first_err), "%s", flam3gpu_last_error());
+      rv = 1;
+    }
+    free(outs[i]);
+    outs[i] = NULL;
+  }
+  if (s) flam3gpu_service_destroy(s);
+  for (int i = 0; i < n; i++) free(outs[i]);
+  free(outs);
+  free(tk);
+  if (rv && first_err[0]) f3g_set_error("%s", first_err);
+  if (rv) fprintf(stderr, "flam3gpu: %s\n", flam3gpu_last_error());
+  return rv;
+}

@@ -167,6 +167,28 @@ def render_batch(frames, field=0, nchan=3, transp=0, **cfg):
     return [(outs[i], stats[i]) for i in range(n)]
 
 
+def render_batch_png(frames, transp=0):
+    """flam3gpu_render_batch_png: the frames rendered as RGBA through one
+    temporary service, each encoded as PNG on the device as it completes;
+    returns a list of (png bytes, stats)."""
+    lib = _lib()
+    n = len(frames)
+    arr = (abi.flam3_frame * n)(*[F.f for F in frames])
+    stats = (abi.stat_struct * n)()
+    pngs = (C.POINTER(C.c_ubyte) * n)()
+    lens = (C.c_size_t * n)()
+    lib.flam3gpu_render_batch_png.argtypes = [C.POINTER(abi.flam3_frame), C.c_int, C.c_int,
+                                              C.POINTER(abi.stat_struct), C.POINTER(C.POINTER(C.c_ubyte)),
+                                              C.POINTER(C.c_size_t)]
+    r = lib.flam3gpu_render_batch_png(arr, n, transp, stats, pngs, lens)
+    for i, F in enumerate(frames):
+        F.f.rc = arr[i].rc
+    out = [(render._take_buffer(pngs[i], lens[i]) if pngs[i] else None, stats[i]) for i in range(n)]
+    if r:
+        raise render.Flam3GpuError("render_batch_png failed: " + lib.flam3gpu_last_error().decode())
+    return out
+
+
 def autotune(frames, quality_scale=0.25):
     lib = _lib()
     n = len(frames)

@@ -299,6 +299,17 @@ int flam3gpu_write_png(FILE *file, void *image, int width, int height, flam3gpu_
 int flam3gpu_render_png(flam3_frame *f, int transp, stat_struct *stats, const char *genome_xml,
                         unsigned char **png, size_t *png_len);
 
+/* flam3-animate's frame loop with PNG output (flam3-animate.c:225-310):
+ * renders the n frames as RGBA (all fields, as flam3gpu_render(f, out,
+ * flam3_field_both, 4, transp, stats) would) through a render service and
+ * encodes each on the device as soon as it completes, while the rest
+ * render.  Each frame's size is its first genome's width x height.
+ * pngs[i] receives a malloc'd PNG (release with free), lens[i] its size,
+ * stats[i] the frame's statistics; the text chunks carry the statistics
+ * (no genome).  Returns 0, or 1 when any frame failed. */
+int flam3gpu_render_batch_png(flam3_frame *frames, int n, int transp, stat_struct *stats, unsigned char **pngs,
+                              size_t *lens);
+
 /* Kernel time (ms, CUDA events) of the calling thread's last PNG encode. */
 int flam3gpu_png_last_ms(double *encode_ms);
 

@@ -206,3 +206,23 @@ def test_render_png_matches_render(gpulib, bpc, transp):
     assert vals["flam3_samples"] == "%g" % st.num_iters
     assert vals["flam3_genome"] == "<flame/>"
     assert render.png_last_ms() > 0
+
+
+@pytest.mark.gpu
+def test_render_batch_png_matches_render_batch(gpulib):
+    from flam3_gb300 import service
+
+    def frames(tag):
+        gs = gm.animation_keys(2, width=192, height=108, quality=30.0, temporal_samples=10)
+        return [gm.Frame(gs, bits=33, seed="bpng-%d" % i, time=float(i)) for i in range(4)]
+
+    got = service.render_batch_png(frames("a"))
+    ref = service.render_batch(frames("a"), nchan=4)
+    for (png, st), (img, st2) in zip(got, ref):
+        pix, F, ihdr, texts = decode(png, img.shape, np.uint8)
+        assert ihdr[:4] == (192, 108, 8, 6)
+        assert np.array_equal(F, _oracle.png_filter(pix))
+        assert float(np.mean(np.abs(pix.astype(np.int64) - img.astype(np.int64)) <= 1)) >= 0.999
+        assert st.num_iters == st2.num_iters
+        vals = {k: v for _, k, v in text_items(texts)}
+        assert vals["flam3_samples"] == "%g" % st.num_iters and vals["flam3_genome"] == ""
