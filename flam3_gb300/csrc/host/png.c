@@ -258,6 +258,17 @@ int flam3gpu_encode_png(const void *image, int image_on_device, int width, int h
   *png = NULL;
   *png_len = 0;
   if (check_image(width, height, nchan, bpc)) return 1;
+  if (ntext < 0 || (ntext > 0 && !text)) {
+    f3g_set_error("bad text chunk list");
+    return 1;
+  }
+  for (int i = 0; i < ntext; i++) {
+    const size_t kl = text[i].key ? strlen(text[i].key) : 0;
+    if (kl < 1 || kl > 79) { /* PNG keywords are 1-79 bytes */
+      f3g_set_error("text chunk %d: keyword must be 1-79 bytes", i);
+      return 1;
+    }
+  }
   f3g_ctx *c = f3g_get_ctx();
   if (!c) {
     f3g_set_error("no CUDA device available");

@@ -97,6 +97,11 @@ def test_encode_argument_checks_without_gpu():
     for w, h, nchan, bpc in [(0, 4, 4, 1), (4, 4, 5, 1), (4, 4, 4, 3), (4, -1, 3, 2)]:
         assert lib.flam3gpu_encode_png(buf, 0, w, h, nchan, bpc, None, 0, C.byref(out), C.byref(n)) == 1
     assert lib.flam3gpu_encode_png(None, 0, 4, 4, 4, 1, None, 0, C.byref(out), C.byref(n)) == 1
+    # text chunk keywords: 1-79 bytes (checked before any device work)
+    bad = (render.PngText * 2)(render.PngText(b"ok", b"x", 0), render.PngText(b"k" * 80, b"x", 0))
+    assert lib.flam3gpu_encode_png(buf, 0, 4, 4, 4, 1, bad, 2, C.byref(out), C.byref(n)) == 1
+    assert b"keyword" in lib.flam3gpu_last_error()
+    assert lib.flam3gpu_encode_png(buf, 0, 4, 4, 4, 1, None, 1, C.byref(out), C.byref(n)) == 1
 
 
 # ---- GPU ----
