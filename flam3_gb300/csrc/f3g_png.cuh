@@ -187,25 +187,28 @@ PNG_HD int match_len(const uint8_t *F, int a, int d, int maxlen) {
 }
 
 /* longest match at p among the candidates, not reaching past end; the
- * search stops at the first match of the greatest possible length */
+ * search stops at the first match of the greatest possible length.  Only
+ * candidates whose first 4 bytes match can reach MIN_MATCH, so one word
+ * compare screens each candidate. */
 PNG_HD int best_match(const uint8_t *F, long long p, long long end, const Cands &C, int &bd) {
   const int maxlen = (int)((end - p) < MAX_MATCH ? (end - p) : MAX_MATCH);
   int bl = 0;
   bd = 0;
+  if (maxlen < MIN_MATCH) return 0;
   const int ip = (int)p;
-  const uint8_t x0 = F[ip];
+  const uint32_t w = load32u(F, ip);
   for (int k = 0; k < C.nd && bl < maxlen; k++) {
     const int d = C.dist[k];
-    if (d > ip || F[ip - d] != x0) continue;
-    const int L = match_len(F, ip, d, maxlen);
+    if (d > ip || load32u(F, ip - d) != w) continue;
+    const int L = 4 + match_len(F, ip + 4, d, maxlen - 4);
     if (L > bl) bl = L, bd = d;
   }
   if (bl < maxlen && p + 4 <= C.total) {
     const uint32_t v = C.wtab[hash4(F + ip)];
     if (v) {
       const long long d = p - (C.wbase + (long long)v - 1);
-      if (d >= 1 && d <= WINDOW && F[ip - d] == x0) {
-        const int L = match_len(F, ip, (int)d, maxlen);
+      if (d >= 1 && d <= WINDOW && load32u(F, ip - (int)d) == w) {
+        const int L = 4 + match_len(F, ip + 4, (int)d, maxlen - 4);
         if (L > bl) bl = L, bd = (int)d;
       }
     }
