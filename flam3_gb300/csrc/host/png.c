@@ -358,9 +358,25 @@ int flam3gpu_png_last_ms(double *encode_ms) {
 
 
 /* flam3-animate's frame loop with PNG output (flam3-animate.c:225-310):
- * the frames render through a render service (all admitted together) and
- * each is encoded on the device as soon as it completes, on this thread's
- * stream while the service renders the rest. */
+ * the frames render through a render service in chunks of up to BATCH_PNG
+ * frames, the next chunk queued before the current one is collected, and
+ * each frame is encoded on the device as soon as it completes, on this
+ * thread's stream while the service renders the rest.  Host memory holds
+ * the raw images of two chunks at most. */
+#define BATCH_PNG 32
+
+static int submit_chunk(flam3gpu_service *s, flam3_frame *frames, int n, int transp, void **outs, uint64_t *tk) {
+  for (int i = 0; i < n; i++) {
+    const flam3_genome *g = &frames[i].genomes[0];
+    outs[i] = malloc((size_t)g->width * g->height * 4 * frames[i].bytes_per_channel);
+    if (!outs[i]) {
+      f3g_set_error("out of host memory");
+      return 1;
+    }
+  }
+  return flam3gpu_service_submit_many(s, frames, n, outs, flam3_field_both, 4, transp, tk);
+}
+
 int flam3gpu_render_batch_png(flam3_frame *frames, int n, int transp, stat_struct *stats, unsigned char **pngs,
                               size_t *lens) {
   f3g_clear_error();
@@ -375,46 +391,45 @@ int flam3gpu_render_batch_png(flam3_frame *frames, int n, int transp, stat_struc
   cfg.round_samples = -1;
   void **outs = (void **)calloc((size_t)n, sizeof(void *));
   uint64_t *tk = (uint64_t *)calloc((size_t)n, sizeof(uint64_t));
-  int rv = 0;
   if (!outs || !tk) {
     f3g_set_error("out of host memory");
     free(outs);
     free(tk);
     return 1;
   }
-  for (int i = 0; i < n && !rv; i++) {
-    const flam3_genome *g = &frames[i].genomes[0];
-    outs[i] = malloc((size_t)g->width * g->height * 4 * frames[i].bytes_per_channel);
-    if (!outs[i]) {
-      f3g_set_error("out of host memory");
-      rv = 1;
-    }
-  }
-  flam3gpu_service *s = rv ? NULL : flam3gpu_service_create(&cfg);
-  if (!rv && !s) rv = 1;
-  if (!rv) rv = flam3gpu_service_submit_many(s, frames, n, outs, flam3_field_both, 4, transp, tk);
+  flam3gpu_service *s = flam3gpu_service_create(&cfg);
+  int rv = s ? 0 : 1;
   char first_err[256] = "";
-  for (int i = 0; i < n && s; i++) {
-    if (!tk[i]) continue;
-    if (flam3gpu_service_wait(s, tk[i], -1, &stats[i], NULL)) {
-      if (!first_err[0]) snprintf(first_err, sizeof(first_err), "%s", flam3gpu_last_error());
-      rv = 1;
-      continue;
+  if (s && submit_chunk(s, frames, n < BATCH_PNG ? n : BATCH_PNG, transp, outs, tk)) rv = 1;
+  for (int c0 = 0; c0 < n && s; c0 += BATCH_PNG) {
+    const int c1 = c0 + BATCH_PNG < n ? c0 + BATCH_PNG : n;
+    /* queue the next chunk first, so the device stays busy */
+    if (!rv && c1 < n) {
+      const int m = c1 + BATCH_PNG < n ? BATCH_PNG : n - c1;
+      if (submit_chunk(s, frames + c1, m, transp, outs + c1, tk + c1)) rv = 1;
     }
-    char badvals[64], numiters[64], rtime[32];
-    snprintf(badvals, sizeof(badvals), "%g", stats[i].badvals / (double)stats[i].num_iters);
-    snprintf(numiters, sizeof(numiters), "%g", (double)stats[i].num_iters);
-    snprintf(rtime, sizeof(rtime), "%d", stats[i].render_seconds);
-    flam3gpu_png_text t[8];
-    const int nt = comment_texts(NULL, badvals, numiters, rtime, t);
-    const flam3_genome *g = &frames[i].genomes[0];
-    if (flam3gpu_encode_png(outs[i], 0, g->width, g->height, 4, frames[i].bytes_per_channel, t, nt, &pngs[i],
-                            &lens[i])) {
-      if (!first_err[0]) snprintf(first_err, sizeof(first_err), "%s", flam3gpu_last_error());
-      rv = 1;
+    for (int i = c0; i < c1; i++) {
+      if (!tk[i]) continue;
+      if (flam3gpu_service_wait(s, tk[i], -1, &stats[i], NULL)) {
+        if (!first_err[0]) snprintf(first_err, sizeof(first_err), "%s", flam3gpu_last_error());
+        rv = 1;
+      } else {
+        char badvals[64], numiters[64], rtime[32];
+        snprintf(badvals, sizeof(badvals), "%g", stats[i].badvals / (double)stats[i].num_iters);
+        snprintf(numiters, sizeof(numiters), "%g", (double)stats[i].num_iters);
+        snprintf(rtime, sizeof(rtime), "%d", stats[i].render_seconds);
+        flam3gpu_png_text t[8];
+        const int nt = comment_texts(NULL, badvals, numiters, rtime, t);
+        const flam3_genome *g = &frames[i].genomes[0];
+        if (flam3gpu_encode_png(outs[i], 0, g->width, g->height, 4, frames[i].bytes_per_channel, t, nt, &pngs[i],
+                                &lens[i])) {
+          if (!first_err[0]) snprintf(first_err, sizeof(first_err), "%s", flam3gpu_last_error());
+          rv = 1;
+        }
+      }
+      free(outs[i]);
+      outs[i] = NULL;
     }
-    free(outs[i]);
-    outs[i] = NULL;
   }
   if (s) flam3gpu_service_destroy(s);
   for (int i = 0; i < n; i++) free(outs[i]);

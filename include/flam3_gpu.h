@@ -301,9 +301,10 @@ int flam3gpu_render_png(flam3_frame *f, int transp, stat_struct *stats, const ch
 
 /* flam3-animate's frame loop with PNG output (flam3-animate.c:225-310):
  * renders the n frames as RGBA (all fields, as flam3gpu_render(f, out,
- * flam3_field_both, 4, transp, stats) would) through a render service and
- * encodes each on the device as soon as it completes, while the rest
- * render.  Each frame's size is its first genome's width x height.
+ * flam3_field_both, 4, transp, stats) would) through a render service, in
+ * chunks of 32 with the next chunk queued before the current one is
+ * collected (host memory: two chunks of raw images), and encodes each on
+ * the device as soon as it completes, while the rest render.  Each frame's size is its first genome's width x height.
  * pngs[i] receives a malloc'd PNG (release with free), lens[i] its size,
  * stats[i] the frame's statistics; the text chunks carry the statistics
  * (no genome).  Returns 0, or 1 when any frame failed. */

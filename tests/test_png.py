@@ -219,7 +219,8 @@ def test_render_batch_png_matches_render_batch(gpulib):
 
     def frames(tag):
         gs = gm.animation_keys(2, width=192, height=108, quality=30.0, temporal_samples=10)
-        return [gm.Frame(gs, bits=33, seed="bpng-%d" % i, time=float(i)) for i in range(4)]
+        # 35 frames: two chunks of the batch pipeline
+        return [gm.Frame(gs, bits=33, seed="bpng-%d" % i, time=float(i)) for i in range(35)]
 
     got = service.render_batch_png(frames("a"))
     ref = service.render_batch(frames("a"), nchan=4)
