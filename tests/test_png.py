@@ -119,6 +119,7 @@ IMAGES = [
     ("one_column", 3000, 1, 3, np.uint8, "render"),
     ("wide_rows", 12, 9001, 4, np.uint8, "render"),      # rows longer than the 32 KB window
     ("segment_edge", 64, 128, 4, np.uint8, "noise"),     # stream of 64 * 513 bytes
+    ("uhd_rgba16", 2160, 3840, 4, np.uint16, "render"),  # 66 MB raw, about 4050 segments
 ]
 
 
