@@ -88,16 +88,15 @@ def build(force=False, verbose=False, defines=(), out=None):
     return lib
 
 
-def build_oracle(with_reference=None):
-    """Builds the test oracle (oracle/liboracle.so) and, where the reference
-    sources exist, oracle/_ref.  Test infrastructure only."""
+def build_oracle(reference=None):
+    """Builds the test oracle (oracle/liboracle.so) and, when `reference`
+    (or the FLAM3_REFERENCE environment variable) names a reference source
+    tree that exists, oracle/_ref from it.  Test infrastructure only."""
     od = os.path.join(ROOT, "oracle")
     make = shutil.which("make")
     subprocess.run([make, "-C", od, "port", "liboracle_fast.so"], check=True, capture_output=True)
-    ref = os.environ.get("FLAM3_REFERENCE", "/root/reference")
-    if with_reference is None:
-        with_reference = os.path.isdir(ref)
-    if with_reference:
+    ref = reference or os.environ.get("FLAM3_REFERENCE")
+    if ref and os.path.isfile(os.path.join(ref, "flam3.c")):
         subprocess.run([make, "-C", od, "ref", "REF=" + ref], check=True, capture_output=True)
 
 

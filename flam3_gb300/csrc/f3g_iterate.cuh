@@ -583,6 +583,19 @@ __global__ void __launch_bounds__(256) k_apply_xform(const F3GPass *__restrict__
   }
 }
 
+/* xform choice of every 14-bit value of every row of a pass's choice table
+ * (the iterate kernel's pick_xform), for comparison with the reference's
+ * 16384-entry rows (flam3.c:76-111, 165-224) */
+static __global__ void __launch_bounds__(256) k_xform_choice(const F3GPass *__restrict__ pass, int rows,
+                                                      uint16_t *out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PassS<float> &s = *reinterpret_cast<PassS<float> *>(smem_raw);
+  stage_pass<float>(s, pass);
+  __syncthreads();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < rows * F3G_GRAIN; k += gridDim.x * blockDim.x)
+    out[k] = (uint16_t)pick_xform<float>(s, k / F3G_GRAIN, (uint32_t)(k % F3G_GRAIN));
+}
+
 static __global__ void __launch_bounds__(256) k_accumulate(const F3GPass *__restrict__ pass, const double *__restrict__ pts,
                                                     long long n) {
   extern __shared__ __align__(16) unsigned char smem_raw[];

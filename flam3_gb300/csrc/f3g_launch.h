@@ -85,6 +85,7 @@ int f3g_launch_fused_log_filter(const void *buckets, int bkind, int W, int H, do
 int f3g_launch_apply_xform(const F3GPass *d_pass, int fn, int n, const double *d_pin, const uint32_t *d_words,
                            int wpp, double *d_qout, int *d_bad, int precision, cudaStream_t st);
 int f3g_launch_accumulate(const F3GPass *d_pass, const double *d_points, long long n, cudaStream_t st);
+int f3g_launch_xform_choice(const F3GPass *d_pass, int rows, uint16_t *d_out, cudaStream_t st);
 int f3g_launch_iterate_chains(const F3GPass *d_pass, int nchains, int n, int fuse, const double *d_starts,
                               uint32_t key0, uint32_t key1, double *d_samples, unsigned long long *d_bad,
                               int precision, cudaStream_t st);

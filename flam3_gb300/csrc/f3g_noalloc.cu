@@ -2,16 +2,24 @@
  * f3g_noalloc.cu -- flam3gpu_render_noalloc: a render that allocates no
  * device memory.
  *
- * Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
- * being built around it, plug-in hosts whose memory pool owns every
- * allocation, processes with a hard device-memory budget fixed at start-up.
- * This entry point takes all of its device scratch -- the histogram (and its
+ * Some callers cannot call cudaMalloc: plug-in hosts whose memory pool owns
+ * every device allocation of the process, and services that fix their
+ * device-memory budget at start-up and must not grow it per request.  This
+ * entry point takes all of its device scratch -- the histogram (and its
  * count plane), the pass tables, the work counters, the filter tables and the
  * staged output image -- from one file-scope static __device__ array of
  * F3G_NOALLOC_BYTES, which the CUDA loader reserves on every device that
  * loads the library and keeps until the process exits.  It calls no
- * cudaMalloc, cudaFree, cudaMallocHost or other allocating CUDA routine, and
- * uses the legacy default stream and no events.
+ * cudaMalloc, cudaFree, cudaMallocHost or other allocating CUDA routine.  Its
+ * copies are blocking cudaMemcpy calls on the legacy default stream, and it
+ * reads the work counters back to the host between the iteration and the
+ * tail, so the call returns only when the image is in the caller's buffer.
+ *
+ * Set-up: the first call on each device looks up the array's device address
+ * with cudaGetSymbolAddress (with that device current) and keeps it for the
+ * rest of the process; make that first call before any stream capture.  A
+ * cudaDeviceReset unloads the module and may move the array, so the entry
+ * point must not be used on a device after that device was reset.
  *
  * Limits: one batch (nbatches == 1), and the render's scratch must fit the
  * array; larger requests are refused with an error naming both sizes.
@@ -144,7 +152,10 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
       f3g_set_error("density estimator filter widths must be >= 0");
       goto done;
     }
-    if (bits <= 32) cp.estimator = 0.0;
+    if (bits <= 32 && cp.estimator > 0.0) {
+      fprintf(stderr, "warning: density estimation disabled with %d bit buffers.\n", bits);
+      cp.estimator = 0.0;
+    }
     if (cp.estimator > 0.0) {
       ks = f3g_de_filters(cp.estimator, cp.estimator_minimum, cp.estimator_curve, g.oversample, &mfc, &mfi, &de_w,
                           &de_c);

@@ -52,6 +52,14 @@ extern "C" int f3g_launch_iterate_chains(const F3GPass *d_pass, int nchains, int
   return (int)cudaGetLastError();
 }
 
+extern "C" int f3g_launch_xform_choice(const F3GPass *d_pass, int rows, uint16_t *d_out, cudaStream_t st) {
+  const size_t smem = sizeof(f3g::PassS<float>);
+  cudaFuncSetAttribute(f3g::k_xform_choice, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int blocks = (rows * F3G_GRAIN + 255) / 256;
+  f3g::k_xform_choice<<<blocks, 256, smem, st>>>(d_pass, rows, d_out);
+  return (int)cudaGetLastError();
+}
+
 /* ---------------------------------------------------------------------
  * Ceiling probe for the iterate kernel's roofline: float4 atomic adds
  * (red.global.add.v4.f32, the bucket update of plot()) at pseudo-random

@@ -193,6 +193,42 @@ out:
   return rc;
 }
 
+int flam3gpu_xform_choice_table(flam3_genome *src, uint16_t *table, int *rows_out) {
+  f3g_clear_error();
+  f3g_ctx *c = f3g_get_ctx();
+  if (!c) {
+    f3g_set_error("no CUDA device available");
+    return 1;
+  }
+  const int ns = src->num_xforms - (src->final_xform_index >= 0);
+  if (ns < 1) {
+    f3g_set_error("the genome has no standard xforms");
+    return 1;
+  }
+  flam3_genome cp;
+  F3GPass *d_pass = NULL;
+  uint16_t *d_out = NULL;
+  int rc = 1;
+  if (prepare_single_pass(c, src, &d_pass, &cp)) goto out;
+  const int rows = 1 + (c->h_passes->chaos_enable ? ns : 0);
+  if (cudaMemcpy(d_pass, c->h_passes, sizeof(F3GPass), cudaMemcpyHostToDevice) != cudaSuccess) goto out;
+  if (cudaMalloc((void **)&d_out, (size_t)rows * F3G_GRAIN * sizeof(uint16_t)) != cudaSuccess) goto out;
+  if (f3g_launch_xform_choice(d_pass, rows, d_out, c->stream)) {
+    f3g_set_error("xform choice launch failed");
+    goto out;
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) goto out;
+  if (cudaMemcpy(table, d_out, (size_t)rows * F3G_GRAIN * sizeof(uint16_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+    goto out;
+  if (rows_out) *rows_out = rows;
+  rc = 0;
+out:
+  if (rc && !flam3gpu_last_error()[0]) f3g_set_error("CUDA error: %s", cudaGetErrorString(cudaGetLastError()));
+  cudaFree(d_out);
+  f3g_genome_free(&cp);
+  return rc;
+}
+
 int f3g_accumulate_impl(flam3_frame *f, int field, const double *points, long n, double *hist, int *hist_w,
                         int *hist_h);
 

@@ -11,6 +11,7 @@
  * reader, not compressed.  Text values that are NULL or empty are written
  * as empty tEXt chunks, as libpng does.
  */
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -25,17 +26,18 @@
 /* ---- chunk writing (host side, a few bytes) ---- */
 
 static uint32_t crc_table[256];
-static int crc_ready = 0;
+static pthread_once_t crc_once = PTHREAD_ONCE_INIT;
 
-static void crc_init(void) {
-  if (crc_ready) return;
+static void crc_fill(void) {
   for (uint32_t i = 0; i < 256; i++) {
     uint32_t c = i;
     for (int k = 0; k < 8; k++) c = (c & 1u) ? (c >> 1) ^ 0xEDB88320u : c >> 1;
     crc_table[i] = c;
   }
-  crc_ready = 1;
 }
+
+/* concurrent writers from several host threads fill the table once */
+static void crc_init(void) { pthread_once(&crc_once, crc_fill); }
 
 static uint32_t crc_update(uint32_t c, const unsigned char *d, size_t n) {
   for (size_t i = 0; i < n; i++) c = crc_table[(c ^ d[i]) & 255u] ^ (c >> 8);

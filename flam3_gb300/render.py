@@ -74,6 +74,7 @@ def load():
                                                C.POINTER(C.c_int)]
     lib.flam3gpu_iterate_chains.argtypes = [G, C.c_int, C.c_int, C.c_int, dp, C.c_uint64, dp,
                                             C.POINTER(C.c_long), C.c_int]
+    lib.flam3gpu_xform_choice_table.argtypes = [G, C.POINTER(C.c_uint16), C.POINTER(C.c_int)]
     lib.flam3gpu_interpolate.argtypes = [G, C.c_int, C.c_double, C.c_double, G]
     lib.flam3gpu_estimate_bounding_box.argtypes = [G, C.c_double, C.c_int, dp, dp, C.POINTER(abi.randctx)]
     lib.flam3gpu_colorhist.argtypes = [G, C.c_int, C.POINTER(abi.randctx), dp]
@@ -226,6 +227,19 @@ def iterate_chains(genome, starts, n, fuse, seed, precision=64):
                                    C.byref(bad), precision):
         _err(lib, "iterate_chains")
     return out, bad.value
+
+
+def xform_choice_table(genome):
+    """The GPU's xform choice for each 14-bit value of each choice row:
+    an (rows, 16384) uint16 array, as flam3_create_xform_distrib's table."""
+    lib = load()
+    g = genome.g
+    ns = g.num_xforms - (1 if g.final_xform_index >= 0 else 0)
+    out = np.zeros((ns + 1) * 16384, np.uint16)
+    rows = C.c_int(0)
+    if lib.flam3gpu_xform_choice_table(C.byref(g), out.ctypes.data_as(C.POINTER(C.c_uint16)), C.byref(rows)):
+        _err(lib, "flam3gpu_xform_choice_table")
+    return out[:rows.value * 16384].reshape(rows.value, 16384)
 
 
 def accumulate_points(frame, points, field=0):

@@ -55,6 +55,15 @@ int flam3gpu_apply_xform(flam3_genome *cp, int fn, int n, const double *p_in,
                          const uint32_t *words, int wpp, double *q_out, int *bad_out,
                          int precision);
 
+/* The GPU's xform choice for every 14-bit random value of every row of the
+ * genome's choice table: table[r*16384 + v] is the xform the iterate kernel
+ * picks for value v in row r (row 0 from the xform weights, row 1+i after
+ * xform i when xaos is on).  Replaces the table flam3_create_xform_distrib
+ * builds (flam3.h:575, flam3.c:165-224), which the kernels hold as
+ * breakpoints; the caller passes room for (standard xforms + 1) * 16384
+ * entries and receives the row count in *rows. */
+int flam3gpu_xform_choice_table(flam3_genome *cp, uint16_t *table, int *rows);
+
 /* GPU bucket accumulation (rect.c:411-516) of a host point stream
  * (n x 4 doubles) for genome f->genomes[0] at f->time; adds into a host FP64
  * 5-channel histogram of the render's geometry.  bits selects the device
@@ -108,19 +117,21 @@ double flam3gpu_lyapunov(flam3_genome *cp, int ntries, randctx *rc);
 int flam3gpu_measure_atomic_rate(long long nbuckets, long long natomics, double *per_second);
 
 /* flam3gpu_render without device allocation.  No counterpart in the
- * reference: for callers that cannot call cudaMalloc (inside CUDA-graph
- * construction, under a host-owned memory pool, with a fixed device-memory
- * budget).  Same arguments, output and errors as flam3gpu_render, but all
- * device scratch (histogram, pass tables, filter tables, staged image) comes
- * from one static device array of flam3gpu_noalloc_capacity() bytes (48 MiB)
- * that every GPU loading the library holds until exit; it calls no cudaMalloc
- * or cudaFree and uses the default stream.  Renders of one batch only, and
- * only those whose scratch fits the array (roughly 1.5 M FP32 or 0.75 M FP64
- * histogram buckets including the gutter); anything larger returns 1 with an
- * error naming the sizes.  Calls share the array: each clears the histogram
- * first, and calls that overlap on the GPU race.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress); make that first
- * call before any stream capture. */
+ * reference: for callers that cannot call cudaMalloc (plug-in hosts whose
+ * memory pool owns every device allocation, services with a device-memory
+ * budget fixed at start-up).  Same arguments, output and errors as
+ * flam3gpu_render, but all device scratch (histogram, pass tables, filter
+ * tables, staged image) comes from one static device array of
+ * flam3gpu_noalloc_capacity() bytes (48 MiB) that every GPU loading the
+ * library holds until exit; it calls no cudaMalloc or cudaFree, and its
+ * copies are blocking cudaMemcpy calls on the legacy default stream.  Renders
+ * of one batch only, and only those whose scratch fits the array (roughly
+ * 1.5 M FP32 or 0.75 M FP64 histogram buckets including the gutter); anything
+ * larger returns 1 with an error naming the sizes.  Calls share the array:
+ * each clears the histogram first, and calls that overlap on the GPU race.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and keeps it; make that first call before any
+ * stream capture, and do not call it on a device after cudaDeviceReset. */
 int flam3gpu_render_noalloc(flam3_frame *f, void *out, int field, int nchan, int transp, stat_struct *stats);
 size_t flam3gpu_noalloc_capacity(void);
 

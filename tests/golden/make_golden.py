@@ -182,7 +182,7 @@ def make_interp(ref):
 def main():
     ref = _oracle.reference(True)
     if ref is None:
-        sys.exit("build the reference first: make -C oracle ref")
+        sys.exit("build the reference first: make -C oracle ref REF=<reference source tree>")
     os.makedirs(OUT, exist_ok=True)
     sections = set(sys.argv[1:]) or {"variations", "renders", "isaac", "filters", "abi", "interp"}
     if "interp" in sections:

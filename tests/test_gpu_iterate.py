@@ -46,6 +46,30 @@ def test_chains_with_final_xform_and_xaos(gpulib):
     np.testing.assert_allclose(gg[:, :4, :2], go[:, :4, :2], rtol=1e-7, atol=1e-9)
 
 
+def test_xform_choice_equals_reference_table(gpulib):
+    """Every 14-bit value of every choice row picks the xform the oracle's
+    16384-entry table holds (flam3.c:76-111, 165-224), with and without
+    xaos, final xforms, and weights that put breakpoints mid-bucket."""
+    import ctypes as C
+
+    lib = _oracle.oracle()
+    rng = np.random.default_rng(11)
+    for trial in range(12):
+        n = int(rng.integers(1, 13))
+        G = gm.random_genome(rng, n, final=bool(trial % 2))
+        if trial % 3 == 0 and n > 1:
+            for i in range(n):
+                for j in range(n):
+                    G.set_chaos(i, j, float(rng.choice([0.0, rng.uniform(0, 2)])))
+                G.set_chaos(i, int(rng.integers(0, n)), 1.0)
+        gpu = render.xform_choice_table(G)
+        ref = lib.f3o_create_xform_distrib(C.byref(G.g))
+        rows = gpu.shape[0]
+        assert rows == 1 + (n if G.g.chaos_enable else 0)
+        want = np.ctypeslib.as_array(ref, shape=(rows * 16384,)).reshape(rows, 16384)
+        np.testing.assert_array_equal(gpu, want)
+
+
 @pytest.mark.parametrize("palette_mode", [0, 1])
 def test_accumulate_matches_oracle(gpulib, palette_mode):
     G = gm.small_genome(1)
