@@ -362,6 +362,18 @@ def resize(genome, width, height):
     g.height = height
 
 
+def crop(genome, width, height, dx=0.0, dy=0.0):
+    """A width x height window of the genome's frame at the same
+    pixels_per_unit (and so the same samples per pixel at a given quality),
+    its centre moved by (dx, dy) output pixels from the frame's centre
+    (rows grow with y, rect.c:785-827)."""
+    g = genome.g
+    g.center[0] += dx / g.pixels_per_unit
+    g.center[1] += dy / g.pixels_per_unit
+    g.width = width
+    g.height = height
+
+
 VARIATIONS_0_19 = list(range(20))
 
 

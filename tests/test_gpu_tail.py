@@ -97,3 +97,43 @@ def test_strip_tail_widths_match_oracle(gpulib, case):
     d = np.abs(out.astype(np.int64) - ref.astype(np.int64))
     assert float(np.mean(d <= 1)) >= 0.999, (cid, fw, float(np.mean(d <= 1)), int(d.max()))
     assert ref.mean() > 1.0
+
+
+# Density estimation at the shapes the workloads use, on 400x300 windows of
+# their own requests (histograms of 800x600 buckets plus the gutter): the
+# config-1 still (DE radius 9, oversample 2, gaussian radius 1: kernels reach
+# about 18 buckets) and the serving trace's 3840x2160 still (DE radius 11,
+# oversample 2: reach about 22), each sparse (most sources take the widest
+# kernels) and denser.
+DE_SHAPE_CASES = [
+    # id, request window, quality
+    ("still_de9_ss2_q40", "still_crop", 40.0),
+    ("still_de9_ss2_q400", "still_crop", 400.0),
+    ("big_de11_ss2_q30", "trace57_big_de11", 30.0),
+    ("big_de11_ss2_q300", "trace57_big_de11", 300.0),
+]
+
+
+@pytest.mark.parametrize("case", DE_SHAPE_CASES, ids=[c[0] for c in DE_SHAPE_CASES])
+def test_de_tail_at_workload_shapes_matches_oracle(gpulib, case):
+    from golden import make_quality_refs as qr
+
+    cid, name, q = case
+    meta = dict(qr.load()[name])
+    meta["w"], meta["h"] = 400, 300
+
+    def mk():
+        G, bits = qr.build(name, meta, quality=q)
+        return gm.Frame(G, bits=bits, nthreads=8, seed="de-shape-" + cid)
+
+    F = mk()
+    g = F.genomes[0].g
+    assert g.spatial_oversample == 2 and g.estimator in (9.0, 11.0)
+    ref, st, ex = _oracle.oracle_render(F, want_hist=True, fast=True)
+    hist = ex["hist"]
+    assert hist.shape[0] >= 600 and hist.shape[1] >= 800
+    out, _, _ = render.render(mk(), hist_in=hist)
+    d = np.abs(out.astype(np.int64) - ref.astype(np.int64))
+    frac_ok = float(np.mean(d <= 1))
+    assert frac_ok >= 0.999, (cid, frac_ok, int(d.max()))
+    assert ref.mean() > 1.0
