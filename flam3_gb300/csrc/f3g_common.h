@@ -107,6 +107,7 @@ typedef struct {
   float dmap[256][4];       /* palette * 255 * color_scalar (rect.c:778-782) */
   int cmap_size;            /* 256 - apo_palette */
   int palette_mode;         /* 0 step, 1 linear */
+  int trunc_hits;           /* integer buckets (bits 32/33): each hit's channels truncated (flam3.c:3688-3703) */
   /* --- camera (rect.c:785-827) ---------------------------------------- */
   double bounds[4];
   double rot[2][2];

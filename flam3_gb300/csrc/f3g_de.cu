@@ -305,6 +305,7 @@ template <bool FUSED> static cudaError_t de_attr_once() {
 extern "C" int f3g_de_prepare(void) {
   cudaError_t e = de_attr_once<true>();
   if (e == cudaSuccess) e = de_attr_once<false>();
+  if (e == cudaSuccess) e = (cudaError_t)f3g_de_bands_prepare();
   return (int)e;
 }
 

@@ -41,7 +41,7 @@ namespace f3g {
 
 template <typename R> struct PassS {
   int num_xforms, num_std, final_index, final_enable, chaos_enable, fuse, mode, full;
-  int width, height, nbuckets, rotate, cmap_size, palette_mode, bucket_kind, S;
+  int width, height, nbuckets, rotate, cmap_size, palette_mode, bucket_kind, S, trunc;
   long long samples, nchunks;
   unsigned long long *counters;
   uint32_t key0, key1;
@@ -71,7 +71,7 @@ __device__ void stage_pass(PassS<R> &s, const F3GPass *__restrict__ p) {
     s.mode = p->iter_mode; s.full = p->full_variations;
     s.width = p->width; s.height = p->height; s.nbuckets = p->width * p->height;
     s.rotate = p->rotate; s.cmap_size = p->cmap_size;
-    s.palette_mode = p->palette_mode; s.bucket_kind = p->bucket_kind;
+    s.palette_mode = p->palette_mode; s.bucket_kind = p->bucket_kind; s.trunc = p->trunc_hits;
     s.samples = p->samples; s.nchunks = p->nchunks; s.key0 = p->key[0]; s.key1 = p->key[1];
     s.b0 = (R)p->bounds[0]; s.b1 = (R)p->bounds[1]; s.b2 = (R)p->bounds[2]; s.b3 = (R)p->bounds[3];
     s.db0 = p->bounds[0]; s.db1 = p->bounds[1]; s.db2 = p->bounds[2]; s.db3 = p->bounds[3];
@@ -201,6 +201,11 @@ __device__ __forceinline__ unsigned plot(const PassS<R> &s, R qx, R qy, R qc, R 
     float o = (float)qo;
     col.x *= o; col.y *= o; col.z *= o; col.w *= o;
     cnt *= o;
+  }
+  if (s.trunc) {
+    /* integer buckets: the reference adds (unsigned)(delta) per hit */
+    col = make_float4(truncf(col.x), truncf(col.y), truncf(col.z), truncf(col.w));
+    cnt = truncf(cnt);
   }
   if (agg) {
     const unsigned act = __activemask();

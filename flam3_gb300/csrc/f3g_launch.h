@@ -23,6 +23,7 @@ typedef struct {
   float highpow;      /* highlight_power */
   float background[3];/* mean background * 256 */
   int nchan, transp, bpc;
+  int trunc_acc;      /* integer accumulator (bits 32): log-scaled and earlyclip values truncated */
 } F3GTonemap;
 
 int f3g_iterate_occupancy(int precision, int full, int mode, int threads);
@@ -35,7 +36,7 @@ int f3g_launch_iterate(const F3GItem *d_items, const long long *d_prefix, int ni
                        F3GCounters *d_ctr, cudaStream_t st);
 
 int f3g_launch_logscale(const void *buckets, int bkind, long long n, double k1, double k2, void *acc, int akind,
-                        cudaStream_t st);
+                        int trunc, cudaStream_t st);
 /* DE kernels take per-kernel constants (4 floats per kernel, see f3g_de.cu) */
 void f3g_de_kernel_info(int mfi, int ks, const double *widths, const double *coefs, float *out);
 int f3g_launch_de(const void *buckets, int bkind, const void *count, int W, int H, int oversample, double k1,
@@ -53,6 +54,22 @@ int f3g_launch_de_fused_tile(const void *buckets, int bkind, const void *count, 
                              double k1, double k2, double curve, int mfc, int mfi, const float *kinfo, int R,
                              int de_offset, const float *filter, int fw, int image_w, int image_h,
                              unsigned char *out, int earlyclip, const F3GTonemap *tp, int tile, cudaStream_t st);
+/* Density estimation by owner bands (f3g_de_bands.cu): classifies every
+ * bucket into fi (W*H bytes) and stores (add = 0) or adds (add = 1) the DE
+ * result into acc (akind: F3G_BK_F32 float4 or F3G_BK_F64 double4 per
+ * bucket).  stats (NULL in renders): device counters [sources, source-band
+ * pairs, taps] the launch adds its work to.  -1 when R or mfi is beyond the
+ * kernel's limits. */
+int f3g_de_bands_supported(int R, int mfi);
+int f3g_de_bands_prepare(void);
+int f3g_launch_de_bands(const void *buckets, int bkind, const void *count, int W, int H, int oversample, double k1,
+                        double k2, double curve, int mfc, int mfi, const float *kinfo, int R, uint8_t *fi, void *acc,
+                        int akind, int add, unsigned long long *stats, cudaStream_t st);
+/* filter + tonemap + pack of an FP32 accumulator (the separable strip kernel
+ * where an instantiation exists, else earlyclip + the 2-D filter kernel) */
+int f3g_launch_acc_filter(void *acc, int W, int H, int de_offset, int oversample, const float *filter, int fw,
+                          int image_w, int image_h, unsigned char *out, int earlyclip, const F3GTonemap *tp,
+                          cudaStream_t st);
 /* raises the tail kernels' shared-memory limits (call before stream capture) */
 int f3g_de_prepare(void);
 int f3g_tail_prepare(void);
@@ -72,6 +89,8 @@ F3G_STRIP_DECL(f32)
 F3G_STRIP_DECL(f64)
 F3G_STRIP_DECL(f32e)
 F3G_STRIP_DECL(f64e)
+F3G_STRIP_DECL(acc)
+F3G_STRIP_DECL(acce)
 #undef F3G_STRIP_DECL
 int f3g_launch_earlyclip(void *acc, int akind, long long n, const F3GTonemap *tp, cudaStream_t st);
 int f3g_launch_filter_tonemap(const void *acc, int akind, int W, int de_offset, int oversample, const float *filter,

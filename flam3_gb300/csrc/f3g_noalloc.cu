@@ -237,6 +237,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
       p->fuse = spec->earlyclip ? 100 : 15;
       p->iter_mode = (cp.chaos_enable || f3g_opts.iter_mode == 0) ? 0 : 1;
       p->bucket_kind = bkind;
+      p->trunc_hits = bits <= 33 && !f3g_opts.float_buckets;
       p->buckets = d_hist;
       f3g_pass_key(spec, p->key);
       batch_samples += p->samples;
@@ -309,6 +310,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     tp.nchan = nchan;
     tp.transp = transp;
     tp.bpc = spec->bytes_per_channel;
+    tp.trunc_acc = bits == 32 && !f3g_opts.float_buckets;
     if (de_on)
       e = f3g_launch_de_fused(d_hist, bkind, use_count ? d_count : nullptr, g.W, g.H, g.oversample, k1, k2,
                               cp.estimator_curve, mfc, mfi, d_de, R, g.de_offset, d_filter,

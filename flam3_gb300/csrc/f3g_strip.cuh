@@ -81,8 +81,11 @@ __device__ __forceinline__ f32x2 x2_mul(f32x2 a, f32x2 b) {
 #endif
 /* Register budget: 65536 / (LS_T * F3G_STRIP_MINB) per thread while a bucket
  * touches at most 5 output rows, 128 above.  EARLY: tonemap each bucket
- * before the filter (flam3's earlyclip) instead of each output pixel. */
-template <int SS, int FW, bool F64, bool EARLY>
+ * before the filter (flam3's earlyclip) instead of each output pixel.  LOG:
+ * the input is the histogram, log-scaled here; without it, the input is an
+ * accumulator that density estimation has already filled with log-scaled
+ * values. */
+template <int SS, int FW, bool F64, bool EARLY, bool LOG = true>
 __global__ void __launch_bounds__(LS_T, (FW / SS <= 5 ? F3G_STRIP_MINB : 4))
     k_log_filter_strip(const void *__restrict__ buckets, int W, int H, float k1, float k2, int de_offset,
                        const float *__restrict__ filter, int image_w, int image_h, int OC, unsigned char *out,
@@ -189,16 +192,29 @@ __global__ void __launch_bounds__(LS_T, (FW / SS <= 5 ? F3G_STRIP_MINB : 4))
           issue_row(n + NS - 1);
 #pragma unroll
           for (int e = 0; e < SS; e++) {
-            float c2, c3;
-            x2_unpack(c23[e], c2, c3);
-            const float ls = log_scale_nz(c3, k1, k2);
-            const f32x2 ls2 = x2_pack(ls, ls);
-            f32x2 v01 = x2_mul(c01[e], ls2), v23 = x2_mul(c23[e], ls2);
+            f32x2 v01 = c01[e], v23 = c23[e];
+            if (LOG) {
+              float c2, c3;
+              x2_unpack(c23[e], c2, c3);
+              const float ls = log_scale_nz(c3, k1, k2);
+              const f32x2 ls2 = x2_pack(ls, ls);
+              v01 = x2_mul(c01[e], ls2);
+              v23 = x2_mul(c23[e], ls2);
+              if (tp.trunc_acc) { /* integer accumulator (bits 32) */
+                float e4[4];
+                x2_unpack(v01, e4[0], e4[1]);
+                x2_unpack(v23, e4[2], e4[3]);
+                v01 = x2_pack(truncf(e4[0]), truncf(e4[1]));
+                v23 = x2_pack(truncf(e4[2]), truncf(e4[3]));
+              }
+            }
             if (EARLY) {
               float e4[4];
               x2_unpack(v01, e4[0], e4[1]);
               x2_unpack(v23, e4[2], e4[3]);
               tonemap(e4, tp);
+              if (tp.trunc_acc)
+                for (int k = 0; k < 4; k++) e4[k] = truncf(e4[k]);
               v01 = x2_pack(e4[0], e4[1]);
               v23 = x2_pack(e4[2], e4[3]);
             }
@@ -272,16 +288,16 @@ static inline int num_sms(void) {
 
 /* resident blocks per SM of one instantiation (queried once, outside any
  * stream capture: f3g_tail_prepare asks for every instantiation) */
-template <int SS, int FW, bool D, bool E>
+template <int SS, int FW, bool D, bool E, bool L = true>
 static int strip_occupancy(void) {
   static int occ = 0;
   if (!occ) {
     int o = 0;
-    cudaFuncSetAttribute(k_log_filter_strip<SS, FW, D, E>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(k_log_filter_strip<SS, FW, D, E, L>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_log_filter_strip<SS, FW, D, E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_log_filter_strip<SS, FW, D, E, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)strip_smem(SS, D, FW));
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_log_filter_strip<SS, FW, D, E>, LS_T,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_log_filter_strip<SS, FW, D, E, L>, LS_T,
                                                       strip_smem(SS, D, FW)) != cudaSuccess ||
         o < 1)
       o = 1;
@@ -293,18 +309,18 @@ static int strip_occupancy(void) {
 /* One wave: as many strips as the resident capacity allows for the column
  * blocks (so every SM holds the same number of rows), with strips of 8 to
  * 32 output rows (shorter ones re-read too much vertical halo). */
-template <int SS, int FW, bool D, bool E>
+template <int SS, int FW, bool D, bool E, bool L = true>
 static int launch_strip(const void *buckets, int W, int H, double k1, double k2, int de_offset, const float *filter,
                         int image_w, int image_h, unsigned char *out, const F3GTonemap *tp, cudaStream_t st) {
   const int OC = LS_T - (FW - SS) / SS;
   const int gx = (image_w + OC - 1) / OC;
-  const int cap = strip_occupancy<SS, FW, D, E>() * num_sms();
+  const int cap = strip_occupancy<SS, FW, D, E, L>() * num_sms();
   int gy = cap / gx;
   const int gmin = (image_h + 31) / 32, gmax = (image_h + 7) / 8;
   if (gy < gmin) gy = gmin;
   if (gy > gmax) gy = gmax;
   if (gy < 1) gy = 1;
-  k_log_filter_strip<SS, FW, D, E><<<dim3(gx, gy), LS_T, strip_smem(SS, D, FW), st>>>(
+  k_log_filter_strip<SS, FW, D, E, L><<<dim3(gx, gy), LS_T, strip_smem(SS, D, FW), st>>>(
       buckets, W, H, (float)k1, (float)k2, de_offset, filter, image_w, image_h, OC, out, *tp);
   return (int)cudaGetLastError();
 }

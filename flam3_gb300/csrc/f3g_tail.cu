@@ -31,12 +31,14 @@ namespace f3g {
  * kernels
  * ------------------------------------------------------------------- */
 __global__ void k_logscale(const void *__restrict__ buckets, int bkind, long long n, float k1, float k2, void *acc,
-                           int akind) {
+                           int akind, int trunc) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     float4 c = load_bucket(buckets, bkind, i);
     if (c.w == 0.0f) continue;
     float ls = log_scale(c.w, k1, k2);
     float4 v = make_float4(c.x * ls, c.y * ls, c.z * ls, c.w * ls);
+    /* integer accumulator (bits 32): each add is truncated */
+    if (trunc) v = make_float4(truncf(v.x), truncf(v.y), truncf(v.z), truncf(v.w));
     if (akind == F3G_BK_F32) {
       float4 *a = (float4 *)acc + i;
       float4 o = *a;
@@ -53,6 +55,8 @@ __global__ void k_earlyclip(void *acc, int akind, long long n, F3GTonemap tp) {
     float4 a = acc_load(acc, akind, i);
     float t[4] = {a.x, a.y, a.z, a.w};
     tonemap(t, tp);
+    if (tp.trunc_acc)
+      for (int k = 0; k < 4; k++) t[k] = truncf(t[k]);
     acc_store(acc, akind, i, make_float4(t[0], t[1], t[2], t[3]));
   }
 }
@@ -99,14 +103,19 @@ __global__ void __launch_bounds__(256) k_fused_log_filter(const void *__restrict
       if (c.w != 0.0f) {
         float ls = log_scale(c.w, k1, k2);
         v = make_float4(c.x * ls, c.y * ls, c.z * ls, c.w * ls);
+        if (tp.trunc_acc) v = make_float4(truncf(v.x), truncf(v.y), truncf(v.z), truncf(v.w));
         if (earlyclip) {
           float t[4] = {v.x, v.y, v.z, v.w};
           tonemap(t, tp);
+          if (tp.trunc_acc)
+            for (int k = 0; k < 4; k++) t[k] = truncf(t[k]);
           v = make_float4(t[0], t[1], t[2], t[3]);
         }
       } else if (earlyclip) {
         float t[4] = {0, 0, 0, 0};
         tonemap(t, tp);
+        if (tp.trunc_acc)
+          for (int k = 0; k < 4; k++) t[k] = truncf(t[k]);
         v = make_float4(t[0], t[1], t[2], t[3]);
       }
     }
@@ -140,8 +149,8 @@ static int grid_for(long long n, int threads) {
 }
 
 extern "C" int f3g_launch_logscale(const void *buckets, int bkind, long long n, double k1, double k2, void *acc,
-                                   int akind, cudaStream_t st) {
-  k_logscale<<<grid_for(n, 256), 256, 0, st>>>(buckets, bkind, n, (float)k1, (float)k2, acc, akind);
+                                   int akind, int trunc, cudaStream_t st) {
+  k_logscale<<<grid_for(n, 256), 256, 0, st>>>(buckets, bkind, n, (float)k1, (float)k2, acc, akind, trunc);
   return (int)cudaGetLastError();
 }
 
@@ -167,7 +176,8 @@ extern "C" int f3g_tail_prepare(void) {
   if (fused_log_attr_done) return 0;
   cudaError_t e = cudaFuncSetAttribute(k_fused_log_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (e != cudaSuccess) return (int)e;
-  if (f3g_strip_prepare_f32() || f3g_strip_prepare_f64() || f3g_strip_prepare_f32e() || f3g_strip_prepare_f64e())
+  if (f3g_strip_prepare_f32() || f3g_strip_prepare_f64() || f3g_strip_prepare_f32e() || f3g_strip_prepare_f64e() ||
+      f3g_strip_prepare_acc() || f3g_strip_prepare_acce())
     return (int)cudaErrorUnknown;
   fused_log_attr_done = 1;
   return 0;
@@ -191,4 +201,20 @@ extern "C" int f3g_launch_fused_log_filter(const void *buckets, int bkind, int W
   k_fused_log_filter<<<grid, block, smem, st>>>(buckets, bkind, W, H, (float)k1, (float)k2, de_offset, oversample,
                                                 filter, fw, image_w, image_h, out, earlyclip, *tp);
   return (int)cudaGetLastError();
+}
+
+extern "C" int f3g_launch_acc_filter(void *acc, int W, int H, int de_offset, int oversample, const float *filter,
+                                     int fw, int image_w, int image_h, unsigned char *out, int earlyclip,
+                                     const F3GTonemap *tp, cudaStream_t st) {
+  int e = f3g_tail_prepare();
+  if (e) return e;
+  e = (earlyclip ? f3g_strip_launch_acce : f3g_strip_launch_acc)(acc, W, H, 0.0, 0.0, de_offset, oversample, filter,
+                                                                 fw, image_w, image_h, out, tp, st);
+  if (e != -2) return e;
+  if (earlyclip) {
+    e = f3g_launch_earlyclip(acc, F3G_BK_F32, (long long)W * H, tp, st);
+    if (e) return e;
+  }
+  return f3g_launch_filter_tonemap(acc, F3G_BK_F32, W, de_offset, oversample, filter, fw, image_w, image_h, out,
+                                   earlyclip, tp, st);
 }

@@ -26,7 +26,7 @@ const char *flam3gpu_last_error(void) { return err_buf; }
 
 const char *flam3gpu_version(void) { return "flam3-gb300 0.1 (sm_103a)"; }
 
-flam3gpu_options f3g_opts = {1, 32, 3, 256, 0, 0, 0, 0, {0}};
+flam3gpu_options f3g_opts = {1, 32, 3, 256, 0, 0, 0, 0, 0, 0, 0, {0}};
 
 void flam3gpu_default_options(flam3gpu_options *o) {
   memset(o, 0, sizeof(*o));
@@ -52,6 +52,10 @@ int flam3gpu_set_options(const flam3gpu_options *o) {
   }
   if (o->shuffle_every < 0 || o->blocks < 0 || o->chain_samples < 0) {
     f3g_set_error("negative option");
+    return 1;
+  }
+  if (o->de_kernel != 0 && o->de_kernel != 1) {
+    f3g_set_error("de_kernel must be 0 or 1");
     return 1;
   }
   if (o->de_tile != 0 && (o->de_tile < 4 || o->de_tile > 64)) {

@@ -105,6 +105,9 @@ typedef struct {
   float *h_stage; size_t h_stage_n; /* pinned staging of small uploads (floats) */
   unsigned char *h_img; size_t h_img_bytes; /* pinned staging of the image */
   float *d_de_w; size_t de_w_bytes;
+  uint8_t *d_fi; size_t fi_bytes; /* DE kernel index per bucket (band DE) */
+  unsigned long long *d_de_stats; size_t de_stats_bytes;
+  double de_work[3];               /* band DE work of the last render (de_stats) */
   float *d_de_c; size_t de_c_bytes;
   double timings[8];
   /* PNG encoder (png.c): scratch, IDAT chunks, their length, host images */

@@ -548,7 +548,15 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
   const int fused_tail = (nbatches == 1) && !(io && io->accum_out);
   int de_used_any = 0;
   /* fused DE tail state (one batch) */
-  int fde = 0, fde_mfc = 0, fde_mfi = 0, fde_R = 0, fde_count = 0;
+  int fde = 0, fde_mfc = 0, fde_mfi = 0, fde_R = 0, fde_count = 0, bands = 0;
+  /* work counters of band DE, when asked for (flam3gpu_options.de_stats) */
+  unsigned long long *de_stats = NULL;
+  memset(c->de_work, 0, sizeof(c->de_work));
+  if (f3g_opts.de_stats) {
+    if (f3g_ensure((void **)&c->d_de_stats, &c->de_stats_bytes, 4 * sizeof(unsigned long long))) goto done;
+    CK(cudaMemsetAsync(c->d_de_stats, 0, 4 * sizeof(unsigned long long), c->stream));
+    de_stats = c->d_de_stats;
+  }
   double fde_k1 = 0, fde_k2 = 0, fde_curve = 0;
 
   for (int batch = 0; batch < nbatches; batch++) {
@@ -595,6 +603,7 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
       p->buckets = c->d_hist;
       p->count = use_count ? c->d_count : NULL;
       p->bucket_kind = bkind;
+      p->trunc_hits = bits <= 33 && !f3g_opts.float_buckets;
       batch_samples += p->samples;
       vibrancy += in->vibrancy;
       gamma += in->gamma;
@@ -769,9 +778,12 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         if (!ok) goto done;
       }
       h2d += (double)nk * 4 * sizeof(float);
-      if (fused_tail && f3g_de_fused_smem_tile(g.oversample, g.filter_width, R, nk, de_tile) <= 220 * 1024) {
-        /* DE, filter, tonemap and pack in one kernel below */
-        fde = 1;
+      bands = f3g_opts.de_kernel == 0 && f3g_de_bands_supported(R, mfi);
+      if (bands && f3g_ensure((void **)&c->d_fi, &c->fi_bytes, (size_t)nb)) goto done;
+      if (fused_tail && (bands || f3g_de_fused_smem_tile(g.oversample, g.filter_width, R, nk, de_tile) <= 220 * 1024)) {
+        /* one batch: band DE into the accumulator, then filter + tonemap +
+         * pack; or DE, filter, tonemap and pack in one fused kernel */
+        fde = bands ? 2 : 1;
         fde_mfc = mfc;
         fde_mfi = mfi;
         fde_R = R;
@@ -789,15 +801,19 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
     CK(cudaEventRecord(c->ev[2], c->stream));
     if (de_on) {
       int R = (int)ceil(de_w[0]) - 1;
-      int e = f3g_launch_de(c->d_hist, bkind, use_count ? c->d_count : NULL, g.W, g.H, g.oversample, k1, k2,
-                            cp.estimator_curve, mfc, mfi, c->d_de_w, R, c->d_acc, bkind, c->stream);
-      launches++;
+      int e = bands ? f3g_launch_de_bands(c->d_hist, bkind, use_count ? c->d_count : NULL, g.W, g.H, g.oversample,
+                                          k1, k2, cp.estimator_curve, mfc, mfi, c->d_de_w, R, c->d_fi, c->d_acc,
+                                          bkind, 1, de_stats, c->stream)
+                    : f3g_launch_de(c->d_hist, bkind, use_count ? c->d_count : NULL, g.W, g.H, g.oversample, k1, k2,
+                                    cp.estimator_curve, mfc, mfi, c->d_de_w, R, c->d_acc, bkind, c->stream);
+      launches += bands ? 2 : 1;
       if (e) {
         f3g_set_error("density estimation launch failed: %s", cudaGetErrorString((cudaError_t)e));
         goto done;
       }
     } else {
-      int e = f3g_launch_logscale(c->d_hist, bkind, nb, k1, k2, c->d_acc, bkind, c->stream);
+      int e = f3g_launch_logscale(c->d_hist, bkind, nb, k1, k2, c->d_acc, bkind, bits == 32 && !f3g_opts.float_buckets,
+                                  c->stream);
       launches++;
       if (e) {
         f3g_set_error("log scaling launch failed: %s", cudaGetErrorString((cudaError_t)e));
@@ -844,9 +860,20 @@ tail_fused:;
     tp.nchan = nchan;
     tp.transp = transp;
     tp.bpc = spec->bytes_per_channel;
+    tp.trunc_acc = bits == 32 && !f3g_opts.float_buckets;
     CK(cudaEventRecord(c->ev[4], c->stream));
     int e;
-    if (fde) {
+    if (fde == 2) {
+      e = f3g_launch_de_bands(c->d_hist, bkind, fde_count ? c->d_count : NULL, g.W, g.H, g.oversample, fde_k1, fde_k2,
+                              fde_curve, fde_mfc, fde_mfi, c->d_de_w, fde_R, c->d_fi, c->d_acc, F3G_BK_F32, 0,
+                              de_stats, c->stream);
+      launches += 2;
+      if (!e) {
+        e = f3g_launch_acc_filter(c->d_acc, g.W, g.H, g.de_offset, g.oversample, c->d_filter, g.filter_width,
+                                  g.image_width, g.image_height, c->d_out, spec->earlyclip, &tp, c->stream);
+        launches++;
+      }
+    } else if (fde) {
       e = f3g_launch_de_fused_tile(c->d_hist, bkind, fde_count ? c->d_count : NULL, g.W, g.H, g.oversample, fde_k1,
                               fde_k2, fde_curve, fde_mfc, fde_mfi, c->d_de_w, fde_R, g.de_offset,
                               c->d_filter, g.filter_width, g.image_width, g.image_height, c->d_out, spec->earlyclip,
@@ -930,6 +957,11 @@ tail_fused:;
     }
   }
   rv = 0;
+  if (de_stats) {
+    unsigned long long w[4];
+    if (cudaMemcpy(w, c->d_de_stats, sizeof(w), cudaMemcpyDeviceToHost) == cudaSuccess)
+      for (int i = 0; i < 3; i++) c->de_work[i] = (double)w[i];
+  }
 
 done:
   c->timings[0] = t_iter;
@@ -960,6 +992,13 @@ double flam3gpu_render_memory_required(flam3_frame *f) {
   int bsz = f->bits == 64 ? 32 : 16;
   double nb = (double)cp->spatial_oversample * cp->spatial_oversample * (double)cp->width * cp->height;
   return nb * bsz * 2.0 + (double)cp->width * cp->height * 4 * 2;
+}
+
+int flam3gpu_last_de_work(double w[3]) {
+  f3g_ctx *c = f3g_get_ctx();
+  if (!c) return 1;
+  for (int i = 0; i < 3; i++) w[i] = c->de_work[i];
+  return 0;
 }
 
 int flam3gpu_last_timings(double t[8]) {

@@ -70,7 +70,7 @@ typedef struct f3g_job {
   size_t bsz, csz;
   long long nb;
   int nbatches, ntemporal, threads, precision;
-  int fused_de, fused_log, need_acc, count_any, tile;
+  int fused_de, fused_log, need_acc, count_any, tile, band_de;
   F3GPass *h_passes;      /* nbatches * ntemporal */
   long long *pass_prefix; /* per batch: ntemporal+1 chunk offsets, concatenated */
   batch_plan *bp;
@@ -83,6 +83,7 @@ typedef struct f3g_job {
   /* device */
   char *d_base;
   void *d_hist, *d_count, *d_acc;
+  uint8_t *d_fi; /* band DE: kernel index per bucket */
   unsigned char *d_out;
   F3GPass *d_passes;
   float *d_filter, *d_kinfo;
@@ -203,6 +204,10 @@ static double now_s(void) {
 }
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+/* the DE "tile" value that selects density estimation by owner bands (the
+ * fused tile kernel takes tile edges of 4 and more) */
+#define DE_BANDS 1
 
 /* ------------------------------------------------------------------ tuning */
 
@@ -404,6 +409,7 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
       ppuy = in->ppuy;
       j->stats.num_iters += in->batch_size;
       p->bucket_kind = j->bkind;
+      p->trunc_hits = bits <= 33 && !f3g_opts.float_buckets;
       batch_samples += p->samples;
       full |= p->full_variations;
       if (p->iter_mode == 0) mode = 0;
@@ -458,9 +464,11 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
     tp->nchan = nchan;
     tp->transp = j->transp;
     tp->bpc = spec->bytes_per_channel;
+    tp->trunc_acc = bits == 32 && !f3g_opts.float_buckets;
   }
-  /* tail shape: one batch -> fused kernels; otherwise accumulate per batch */
-  j->tile = 16;
+  /* tail shape: one batch -> band DE + filter, or fused kernels; otherwise
+   * accumulate per batch */
+  j->tile = f3g_opts.de_kernel == 0 ? DE_BANDS : 16;
   int tS = 0, tTile = 0;
   if (use_tuning && force_S <= 0) {
     char key[96];
@@ -490,8 +498,18 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
     }
   }
   if (force_tile > 0) j->tile = force_tile;
+  int de_any = 0, bands_ok = 1;
+  for (int b = 0; b < nbatches; b++)
+    if (j->bp[b].de_on) {
+      de_any = 1;
+      bands_ok &= f3g_de_bands_supported(j->bp[b].R, j->bp[b].mfi);
+    }
+  j->band_de = de_any && bands_ok && j->tile == DE_BANDS;
+  if (j->tile == DE_BANDS && !j->band_de) j->tile = 16;
   if (nbatches == 1) {
-    if (j->bp[0].de_on) {
+    if (j->bp[0].de_on && j->band_de) {
+      /* band DE into the accumulator, then the filter pass */
+    } else if (j->bp[0].de_on) {
       j->fused_de = f3g_de_fused_smem_tile(g.oversample, g.filter_width, j->bp[0].R, j->bp[0].nk, j->tile) <=
                     220 * 1024;
       if (!j->fused_de && j->tile != 16 &&
@@ -506,7 +524,8 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
   j->out_bytes = (size_t)g.image_width * g.image_height * nchan * spec->bytes_per_channel;
   j->dev_bytes = align256((size_t)npass * sizeof(F3GPass)) + align256((size_t)j->nb * j->bsz) +
                  (j->count_any ? align256((size_t)j->nb * j->csz) : 0) +
-                 (j->need_acc ? align256((size_t)j->nb * j->bsz) : 0) + align256(j->out_bytes) +
+                 (j->need_acc ? align256((size_t)j->nb * j->bsz) : 0) + (j->band_de ? align256((size_t)j->nb) : 0) +
+                 align256(j->out_bytes) +
                  align256(F3G_FILTER_FLOATS(g.filter_width) * sizeof(float)) +
                  align256(j->nkinfo * sizeof(float)) + 256;
   rv = 0;
@@ -683,6 +702,7 @@ static int admit_job(flam3gpu_service *s, f3g_job *j) {
   CARVE(j->d_hist, void *, (size_t)j->nb * j->bsz);
   if (j->count_any) CARVE(j->d_count, void *, (size_t)j->nb * j->csz);
   if (j->need_acc) CARVE(j->d_acc, void *, (size_t)j->nb * j->bsz);
+  if (j->band_de) CARVE(j->d_fi, uint8_t *, (size_t)j->nb);
   CARVE(j->d_out, unsigned char *, j->out_bytes);
   CARVE(j->d_filter, float *, F3G_FILTER_FLOATS(j->g.filter_width) * sizeof(float));
   CARVE(j->d_kinfo, float *, j->nkinfo * sizeof(float));
@@ -792,7 +812,18 @@ static int enqueue_tail_ops(flam3gpu_service *s, f3g_job *j, cudaStream_t st, ch
   const flam3_frame *spec = &j->spec;
   int e = 0;
   char tag[32];
-  if (j->fused_de) {
+  if (j->band_de && j->nbatches == 1) {
+    e = f3g_launch_de_bands(j->d_hist, j->bkind, b->use_count ? j->d_count : NULL, g->W, g->H, g->oversample, b->k1,
+                            b->k2, b->curve, b->mfc, b->mfi, j->d_kinfo + b->kinfo_off, b->R, j->d_fi, j->d_acc,
+                            F3G_BK_F32, 0, NULL, st);
+    s->c_launches += 2;
+    if (!e) {
+      e = f3g_launch_acc_filter(j->d_acc, g->W, g->H, g->de_offset, g->oversample, j->d_filter, g->filter_width,
+                                g->image_width, g->image_height, j->d_out, spec->earlyclip, &j->tp, st);
+      s->c_launches++;
+    }
+    snprintf(tag, sizeof(tag), "B");
+  } else if (j->fused_de) {
     e = f3g_launch_de_fused_tile(j->d_hist, j->bkind, b->use_count ? j->d_count : NULL, g->W, g->H, g->oversample,
                                  b->k1, b->k2, b->curve, b->mfc, b->mfi, j->d_kinfo + b->kinfo_off, b->R,
                                  g->de_offset, j->d_filter, g->filter_width, g->image_width, g->image_height,
@@ -806,11 +837,15 @@ static int enqueue_tail_ops(flam3gpu_service *s, f3g_job *j, cudaStream_t st, ch
     s->c_launches++;
     snprintf(tag, sizeof(tag), "L");
   } else {
-    if (b->de_on)
+    if (b->de_on && j->band_de)
+      e = f3g_launch_de_bands(j->d_hist, j->bkind, b->use_count ? j->d_count : NULL, g->W, g->H, g->oversample, b->k1,
+                              b->k2, b->curve, b->mfc, b->mfi, j->d_kinfo + b->kinfo_off, b->R, j->d_fi, j->d_acc,
+                              j->bkind, 1, NULL, st);
+    else if (b->de_on)
       e = f3g_launch_de(j->d_hist, j->bkind, b->use_count ? j->d_count : NULL, g->W, g->H, g->oversample, b->k1, b->k2,
                         b->curve, b->mfc, b->mfi, j->d_kinfo + b->kinfo_off, b->R, j->d_acc, j->bkind, st);
     else
-      e = f3g_launch_logscale(j->d_hist, j->bkind, j->nb, b->k1, b->k2, j->d_acc, j->bkind, st);
+      e = f3g_launch_logscale(j->d_hist, j->bkind, j->nb, b->k1, b->k2, j->d_acc, j->bkind, j->tp.trunc_acc, st);
     s->c_launches++;
     snprintf(tag, sizeof(tag), "%c", b->de_on ? 'D' : 'S');
     if (!e && !final) {
@@ -1696,7 +1731,8 @@ int flam3gpu_autotune(flam3_frame *frames, int n, double quality_scale) {
     return -1;
   }
   static const int S_cand[] = {128, 256, 512, 1024};
-  static const int T_cand[] = {8, 16, 32};
+  /* DE tail shapes: owner bands, or the fused tile kernel at three edges */
+  static const int T_cand[] = {DE_BANDS, 8, 16, 32};
   for (int i = 0; i < n; i++) {
     /* class key of the frame as submitted */
     f3g_job probe;
@@ -1711,7 +1747,7 @@ int flam3gpu_autotune(flam3_frame *frames, int n, double quality_scale) {
     }
     char key[96];
     tune_key(&probe, key, sizeof(key));
-    const int has_de = probe.fused_de;
+    const int has_de = probe.fused_de || probe.band_de;
     job_free_plan(&probe);
     int S0, T0;
     if (tune_lookup(key, &S0, &T0)) continue;
@@ -1723,9 +1759,9 @@ int flam3gpu_autotune(flam3_frame *frames, int n, double quality_scale) {
       if (quality_scale > 0) f.genomes[k].sample_density *= quality_scale;
     }
     double best = 1e300;
-    int bestS = 256, bestT = 16;
+    int bestS = 256, bestT = f3g_opts.de_kernel == 0 ? DE_BANDS : 16;
     for (size_t a = 0; a < sizeof(S_cand) / sizeof(S_cand[0]); a++) {
-      double t = time_job(&f, 3, S_cand[a], 16, NULL);
+      double t = time_job(&f, 3, S_cand[a], 0, NULL);
       if (t > 0 && t < best) {
         best = t;
         bestS = S_cand[a];

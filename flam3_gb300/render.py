@@ -32,7 +32,8 @@ class RenderIO(C.Structure):
 class Options(C.Structure):
     _fields_ = [("iter_mode", C.c_int), ("iter_precision", C.c_int), ("shuffle_every", C.c_int),
                 ("threads_per_block", C.c_int), ("blocks", C.c_int), ("chain_samples", C.c_int),
-                ("seed_salt", C.c_uint64), ("de_tile", C.c_int), ("reserved", C.c_int * 7)]
+                ("seed_salt", C.c_uint64), ("de_tile", C.c_int), ("de_kernel", C.c_int),
+                ("de_stats", C.c_int), ("float_buckets", C.c_int), ("reserved", C.c_int * 4)]
 
 
 class PngText(C.Structure):
@@ -67,6 +68,7 @@ def load():
     lib.flam3gpu_get_options.argtypes = [C.POINTER(Options)]
     lib.flam3gpu_default_options.argtypes = [C.POINTER(Options)]
     lib.flam3gpu_last_timings.argtypes = [dp]
+    lib.flam3gpu_last_de_work.argtypes = [dp]
     lib.flam3gpu_histogram_dims.argtypes = [F, C.c_int] + [C.POINTER(C.c_int)] * 5
     lib.flam3gpu_apply_xform.argtypes = [G, C.c_int, C.c_int, dp, C.POINTER(C.c_uint32), C.c_int, dp,
                                          C.POINTER(C.c_int), C.c_int]
@@ -181,6 +183,14 @@ def last_timings():
     load().flam3gpu_last_timings(t)
     return {"iterate_ms": t[0], "de_ms": t[1], "tail_ms": t[2], "wall_ms": t[3], "launches": int(t[4]),
             "h2d_bytes": int(t[5]), "d2h_bytes": int(t[6]), "plotted": int(t[7])}
+
+
+def last_de_work():
+    """Band density estimation work of the last render (set_options(de_stats=1)
+    first): sources, source-band pairs, taps."""
+    w = (C.c_double * 3)()
+    load().flam3gpu_last_de_work(w)
+    return {"sources": int(w[0]), "pairs": int(w[1]), "taps": int(w[2])}
 
 
 def get_options():

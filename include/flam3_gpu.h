@@ -331,7 +331,15 @@ const char *flam3gpu_version(void);
  * automatic.  chain_samples: samples per chain before a restart with a new
  * random point and fuse (0 = f->sub_batch_size, like the reference).
  * de_tile: output pixels per tile edge of the fused density-estimation
- * kernel (8 .. 32; 0 = 16). */
+ * kernel (8 .. 32; 0 = 16).  de_kernel: 0 = density estimation by owner
+ * bands (register accumulators, no atomics; default), 1 = the fused tile
+ * kernel (DE, filter and tonemap in one pass, shared-memory scatter).
+ * de_stats: 1 = band DE runs an instrumented variant that counts its work
+ * (sources, source-band pairs, taps), read with flam3gpu_last_de_work.
+ * float_buckets: 0 = the reference's integer arithmetic for bits 32 and 33
+ * (each hit's channels truncated before the add, and for bits 32 the
+ * log-scaled accumulator truncated too, flam3.c:3642-3647, 3688-3703,
+ * 3771-3856); 1 = exact FP32 sums (more accurate than the reference). */
 typedef struct {
   int iter_mode;
   int iter_precision;
@@ -341,7 +349,10 @@ typedef struct {
   int chain_samples;
   uint64_t seed_salt;
   int de_tile;        /* output-tile edge of the fused DE kernel (0 = 16) */
-  int reserved[7];
+  int de_kernel;      /* 0 owner bands (default), 1 fused tile */
+  int de_stats;       /* 1: band DE counts its work (flam3gpu_last_de_work) */
+  int float_buckets;  /* 1: bits 32/33 keep exact FP32 sums (no per-hit truncation) */
+  int reserved[4];
 } flam3gpu_options;
 
 void flam3gpu_default_options(flam3gpu_options *o);
@@ -355,6 +366,13 @@ void flam3gpu_get_options(flam3gpu_options *o);
  * launches, [5] host-to-device bytes, [6] device-to-host bytes, [7] samples
  * plotted by the iterate kernels. */
 int flam3gpu_last_timings(double t[8]);
+
+/* Work of the last render's band density estimation on this thread (no
+ * counterpart in the reference), counted only while the de_stats option is
+ * set: [0] sources (non-empty buckets inside the DE bounds), [1] source x
+ * 8-row-band pairs the kernel processed, [2] kernel taps (bucket updates
+ * inside the kernels' discs). */
+int flam3gpu_last_de_work(double w[3]);
 
 /* Replaces flam3_interpolate (flam3.h:562, flam3.c:717-802): the genome at
  * `time` between control points cps[0..ncps-1] (sorted by time), with the

@@ -31,8 +31,8 @@ chi-square test with the warp's 32-fold correlation holds both modes to the
 weights.  The two modes' images sit at the same error against the 16x
 render.
 
-bits=32 (u32 buckets in the reference, density estimation off,
-flam3.c:3642-3647, rect.c:716-719) renders like the oracle's bits=32; the
+bits=32 (u32 buckets and accumulator in the reference, density estimation
+off, flam3.c:3642-3647, 3771-3790) renders like the oracle's bits=32; the
 strip loop of flam3-render (flam3-render.c:311-345) on the GPU matches the
 same loop over the oracle."""
 import math
@@ -123,7 +123,9 @@ def test_xform_choice_frequencies_chi_square(gpulib, mode):
     render.set_options(iter_mode=mode)
     try:
         G = disc_genome(weights)
-        _, st, ex = render.render(gm.Frame(G, bits=33, seed="discs-%d" % mode), want_hist=True)
+        # FP64 buckets count every hit exactly (an FP32 count channel rounds
+        # once a bucket passes 2^24)
+        _, st, ex = render.render(gm.Frame(G, bits=64, seed="discs-%d" % mode), want_hist=True)
     finally:
         render.reset_options()
     counts = disc_counts(ex["hist"], G, n)
@@ -173,11 +175,15 @@ def test_bits32_matches_oracle_bits32(gpulib):
     assert sg.num_iters == so.num_iters
     e_o, e_g = mae(o, ref), mae(g, ref)
     assert e_g <= min(1.1 * e_o + 0.05, e_o + 0.5), (e_g, e_o)
-    # the same genome without DE at bits 33 renders the same picture
-    G = mk(q)
-    G.g.estimator = 0.0
-    g33, _ = render.render(gm.Frame(G, bits=33, seed="b32-g"))
-    assert mae(g33, ref) <= min(1.1 * e_o + 0.05, e_o + 0.5)
+    # the reference's integer accumulator drops log-scaled values below one
+    # unit (the dim parts of the image); exact FP32 sums keep them and so sit
+    # far from the reference's picture
+    render.set_options(float_buckets=1)
+    try:
+        gf, _ = render.render(gm.Frame(mk(q), bits=32, seed="b32-g"))
+    finally:
+        render.reset_options()
+    assert mae(gf, ref) > e_g + 0.5, (mae(gf, ref), e_g)
     assert ref.mean() > 5.0
 
 

@@ -26,6 +26,10 @@ CASES = [
     ("de2_ss3", 2, 33, 2.0, 3, 0, 3, 0, 1, 0, 0),
     ("de9_early", 3, 33, 9.0, 1, 1, 3, 0, 1, 0, 0),
     ("de4_rgba_transp", 4, 64, 4.0, 1, 0, 4, 1, 1, 0, 0),
+    # bits 32: the reference's integer accumulator (DE switched off)
+    ("b32", 0, 32, 0.0, 1, 0, 3, 0, 1, 0, 0),
+    ("b32_early_ss2", 1, 32, 3.0, 2, 1, 3, 0, 1, 0, 0),
+    ("b32_rgba_16", 2, 32, 0.0, 1, 0, 4, 1, 2, 0, 0),
 ]
 
 
@@ -47,15 +51,24 @@ def levels(a, b):
     return np.abs(a - b)
 
 
-@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
-def test_tail_matches_oracle_on_same_histogram(gpulib, case):
+# density estimation runs by owner bands (de_kernel 0, the default) or in the
+# fused tile kernel (1): the DE cases run both
+TAIL_PARAMS = [(c, 0) for c in CASES] + [(c, 1) for c in CASES if c[3] > 0 and c[2] != 32]
+
+
+@pytest.mark.parametrize("case,de_kernel", TAIL_PARAMS, ids=["%s-k%d" % (c[0], k) for c, k in TAIL_PARAMS])
+def test_tail_matches_oracle_on_same_histogram(gpulib, case, de_kernel):
     cid, seed, bits, est, ss, early, nchan, transp, bpc, field, filt = case
     F = frame(seed, bits, est, ss, early, bpc, filt)
     ref, st, ex = _oracle.oracle_render(F, field=field, nchan=nchan, transp=transp, want_hist=True)
     hist = ex["hist"]
     assert hist[..., 4].sum() > 0
     F2 = frame(seed, bits, est, ss, early, bpc, filt)
-    out, st2, _ = render.render(F2, field=field, nchan=nchan, transp=transp, hist_in=hist)
+    render.set_options(de_kernel=de_kernel)
+    try:
+        out, st2, _ = render.render(F2, field=field, nchan=nchan, transp=transp, hist_in=hist)
+    finally:
+        render.reset_options()
     d = np.abs(out.astype(np.int64) - ref.astype(np.int64))
     if bpc == 2:
         d = d // 256
@@ -112,10 +125,11 @@ DE_SHAPE_CASES = [
     ("big_de11_ss2_q30", "trace57_big_de11", 30.0),
     ("big_de11_ss2_q300", "trace57_big_de11", 300.0),
 ]
+DE_SHAPE_PARAMS = [(c, k) for c in DE_SHAPE_CASES for k in (0, 1)]
 
 
-@pytest.mark.parametrize("case", DE_SHAPE_CASES, ids=[c[0] for c in DE_SHAPE_CASES])
-def test_de_tail_at_workload_shapes_matches_oracle(gpulib, case):
+@pytest.mark.parametrize("case,de_kernel", DE_SHAPE_PARAMS, ids=["%s-k%d" % (c[0], k) for c, k in DE_SHAPE_PARAMS])
+def test_de_tail_at_workload_shapes_matches_oracle(gpulib, case, de_kernel):
     from golden import make_quality_refs as qr
 
     cid, name, q = case
@@ -132,8 +146,38 @@ def test_de_tail_at_workload_shapes_matches_oracle(gpulib, case):
     ref, st, ex = _oracle.oracle_render(F, want_hist=True, fast=True)
     hist = ex["hist"]
     assert hist.shape[0] >= 600 and hist.shape[1] >= 800
-    out, _, _ = render.render(mk(), hist_in=hist)
+    render.set_options(de_kernel=de_kernel)
+    try:
+        out, _, _ = render.render(mk(), hist_in=hist)
+    finally:
+        render.reset_options()
     d = np.abs(out.astype(np.int64) - ref.astype(np.int64))
     frac_ok = float(np.mean(d <= 1))
     assert frac_ok >= 0.999, (cid, frac_ok, int(d.max()))
     assert ref.mean() > 1.0
+
+
+def test_band_de_work_counters_and_repeatability(gpulib):
+    """The instrumented band kernel gives the same image as the plain one on
+    the same histogram, and counts its work: every source is one non-empty
+    bucket inside the DE bounds, every tap lies inside a kernel disc; two runs
+    of the plain kernel on one histogram are identical bit for bit (each
+    bucket is added to by one owner in list order)."""
+    F = frame(1, 33, 5.0, 2, 0, 1, 0, w=160, h=120, q=60.0)
+    ref, st, ex = _oracle.oracle_render(F, want_hist=True)
+    hist = ex["hist"]
+    outs = []
+    for stats in (0, 0, 1):
+        render.set_options(de_stats=stats)
+        try:
+            out, _, _ = render.render(frame(1, 33, 5.0, 2, 0, 1, 0, w=160, h=120, q=60.0), hist_in=hist)
+        finally:
+            render.reset_options()
+        outs.append(out)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+    w = render.last_de_work()
+    H, W = hist.shape[:2]
+    inside = hist[1:H - 1, 1:W - 1, 4] > 0  # oversample 2: the DE bounds drop one row and column each side
+    assert w["sources"] == int(inside.sum()), (w, int(inside.sum()))
+    assert w["pairs"] >= w["sources"] and 0 < w["taps"] <= 256 * w["pairs"]
