@@ -178,6 +178,7 @@ def test_band_de_work_counters_and_repeatability(gpulib):
     np.testing.assert_array_equal(outs[0], outs[2])
     w = render.last_de_work()
     H, W = hist.shape[:2]
-    inside = hist[1:H - 1, 1:W - 1, 4] > 0  # oversample 2: the DE bounds drop one row and column each side
+    # oversample 2: the DE bounds are columns [1, W-1) and rows [1, H) (rect.c:79-80, 979)
+    inside = hist[1:H, 1:W - 1, 4] > 0
     assert w["sources"] == int(inside.sum()), (w, int(inside.sum()))
     assert w["pairs"] >= w["sources"] and 0 < w["taps"] <= 256 * w["pairs"]
