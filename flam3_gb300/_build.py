@@ -98,6 +98,9 @@ def build_oracle(reference=None):
     ref = reference or os.environ.get("FLAM3_REFERENCE")
     if ref and os.path.isfile(os.path.join(ref, "flam3.c")):
         subprocess.run([make, "-C", od, "ref", "REF=" + ref], check=True, capture_output=True)
+        if os.path.exists(LIB):
+            # the reference's CLIs relinked onto libflam3gpu (the drop-in)
+            subprocess.run([make, "-C", od, "dropin", "REF=" + ref], check=True, capture_output=True)
 
 
 if __name__ == "__main__":

@@ -74,7 +74,7 @@ static int prepare_single_pass(f3g_ctx *c, flam3_genome *src, F3GPass **d_pass, 
   f3g_genome_copy(cp, src);
   if (f3g_prepare_precalc_flags(cp)) return 1;
   for (int i = 0; i < cp->num_xforms; i++) f3g_xform_precalc(cp, i);
-  if (ensure_host_pass_one(c)) return 1;
+  if (f3g_ensure_host_pass_one(c)) return 1;
   F3GPass *p = c->h_passes;
   memset(p, 0, sizeof(*p));
   if (cp->num_xforms - (cp->final_xform_index >= 0) > 0 && f3g_build_distrib(cp, p)) return 1;
@@ -84,7 +84,7 @@ static int prepare_single_pass(f3g_ctx *c, flam3_genome *src, F3GPass **d_pass, 
   return 0;
 }
 
-int ensure_host_pass_one(f3g_ctx *c) {
+int f3g_ensure_host_pass_one(f3g_ctx *c) {
   if (c->h_passes && c->h_passes_bytes >= sizeof(F3GPass)) return 0;
   if (c->h_passes) cudaFreeHost(c->h_passes);
   c->h_passes = NULL;

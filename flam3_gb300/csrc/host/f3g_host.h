@@ -118,7 +118,7 @@ typedef struct {
 } f3g_ctx;
 
 f3g_ctx *f3g_get_ctx(void);
-int ensure_host_pass_one(f3g_ctx *c);
+int f3g_ensure_host_pass_one(f3g_ctx *c);
 int f3g_ensure(void **ptr, size_t *cap, size_t need);
 extern flam3gpu_options f3g_opts;
 /* samples per thread per chunk for a pass of `samples` samples */

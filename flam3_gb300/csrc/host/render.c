@@ -459,17 +459,22 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
   double wall0 = now_s();
   time_t tstart = time(NULL);
   int bits = spec->bits;
+  /* failures before any state exists: message on stderr, return 1 (the
+   * reference prints its argument errors, flam3.c:3889-3892) */
   if (bits != 32 && bits != 33 && bits != 64) {
     f3g_set_error("flam3: bits must be 32, 33, or 64 not %d.", bits);
+    fprintf(stderr, "flam3gpu: %s\n", flam3gpu_last_error());
     return 1;
   }
   if (nchan != 3 && nchan != 4) {
     f3g_set_error("nchan must be 3 or 4, not %d", nchan);
+    fprintf(stderr, "flam3gpu: %s\n", flam3gpu_last_error());
     return 1;
   }
   f3g_ctx *c = f3g_get_ctx();
   if (!c) {
     f3g_set_error("no CUDA device available");
+    fprintf(stderr, "flam3gpu: %s\n", flam3gpu_last_error());
     return 1;
   }
   stats->num_iters = 0;
@@ -1033,7 +1038,7 @@ int f3g_accumulate_impl(flam3_frame *f, int field, const double *points, long n,
     rv = 0;
     goto done;
   }
-  if (ensure_host_pass_one(c)) goto done;
+  if (f3g_ensure_host_pass_one(c)) goto done;
   F3GPass *p = c->h_passes;
   memset(p, 0, sizeof(*p));
   const char *ap = getenv("apo_palette");
