@@ -44,6 +44,7 @@
 #define DEB_LCAP 2048 /* sources of one chunk (a chunk never holds more positions) */
 #define DEB_Q (DEB_LCAP / DEB_THREADS)
 #define DEB_MAX_REACH 40
+#define DEB_WROWS (DEB_TH + 2 * DEB_MAX_REACH) /* rows of the widest source window */
 #define DEB_NOSRC 0xFFu
 
 namespace f3g {
@@ -103,30 +104,37 @@ struct DEBands {
  * taps inside the kernels' discs) for the roofline; the render uses the
  * plain instantiation. */
 template <bool STATS>
-__global__ void __launch_bounds__(DEB_THREADS) k_de_bands(DEBands P) {
+__global__ void __launch_bounds__(DEB_THREADS, 4) k_de_bands(DEBands P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float4 *sv = (float4 *)smem_raw;                  /* DEB_LCAP log-scaled channels */
-  uint32_t *sxyk = (uint32_t *)(sv + DEB_LCAP);     /* column | row << 8 | kernel << 16 */
+  uint32_t *sxyk = (uint32_t *)(sv + DEB_LCAP);     /* column | row << 8 | kernel << 16 | reach << 24 */
   float4 *kin = (float4 *)(sxyk + DEB_LCAP);        /* nk kernels */
   uint8_t *sfi = (uint8_t *)(kin + P.nk);           /* the chunk's kernel bytes */
-  int *rowstart = (int *)(sfi + DEB_LCAP);          /* list index of each chunk row, + total */
-  int *wsum = rowstart + DEB_LCAP / DEB_TW + 2;     /* per-warp counts of the scan */
+  int *rowstart = (int *)(sfi + DEB_LCAP);          /* list index of each window row, + total */
+  int *rowreach = rowstart + DEB_WROWS + 1;         /* widest reach among each row's sources */
+  int *wsum = rowreach + DEB_WROWS + 1;             /* per-warp counts of the scan */
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int R = P.R, X0 = blockIdx.x * DEB_TW, Y0 = blockIdx.y * DEB_TH;
   const int WX0 = X0 - R, WY0 = Y0 - R, WW = DEB_TW + 2 * R, WH = DEB_TH + 2 * R;
-  const int CH = DEB_LCAP / WW;
+  /* chunks are column slices of the window over all its rows, so every
+   * chunk feeds every band (row slices would leave the warps of the far
+   * bands idle at each chunk's barrier) */
+  const int CW = DEB_LCAP / WH;
   const int B0 = Y0 + DEB_ROWS * warp; /* this warp's first row */
   for (int k = tid; k < P.nk; k += DEB_THREADS) kin[k] = P.kinfo[k];
   float acc[DEB_ROWS][4];
 #pragma unroll
   for (int r = 0; r < DEB_ROWS; r++) acc[r][0] = acc[r][1] = acc[r][2] = acc[r][3] = 0.0f;
   unsigned long long n_pairs = 0, n_taps = 0;
+  /* window rows whose sources can reach this warp's band */
+  const int rlo = max(0, B0 - R - WY0), rhi = min(WH - 1, B0 + DEB_ROWS - 1 + R - WY0);
 
-  for (int cr0 = 0; cr0 < WH; cr0 += CH) {
-    const int rows = min(CH, WH - cr0), npos = rows * WW;
-    /* 1. the chunk's kernel bytes */
+  for (int cc0 = 0; cc0 < WW; cc0 += CW) {
+    const int cols = min(CW, WW - cc0), npos = WH * cols;
+    /* 1. the chunk's kernel bytes, row-major */
+    for (int k = tid; k < WH; k += DEB_THREADS) rowreach[k] = -1;
     for (int k = tid; k < npos; k += DEB_THREADS) {
-      const int bx = WX0 + k % WW, by = WY0 + cr0 + k / WW;
+      const int bx = WX0 + cc0 + k % cols, by = WY0 + k / cols;
       sfi[k] = (bx >= 0 && bx < P.W && by >= 0 && by < P.H) ? P.fi[(long long)by * P.W + bx] : (uint8_t)DEB_NOSRC;
     }
     __syncthreads();
@@ -148,51 +156,59 @@ __global__ void __launch_bounds__(DEB_THREADS) k_de_bands(DEBands P) {
     if (tid == DEB_THREADS - 1) {
       int total = 0;
       for (int w = 0; w < DEB_WARPS; w++) total += wsum[w];
-      rowstart[rows] = total;
+      rowstart[WH] = total;
     }
-    /* 3. records: position, kernel, log-scaled channels (rect.c:120-123) */
+    /* 3. records: position, kernel, reach, log-scaled channels (rect.c:120-123) */
 #pragma unroll
     for (int q = 0; q < DEB_Q; q++) {
       const int p = p0 + q;
       if (p >= npos) break;
-      const int col = p % WW, r = p / WW;
-      if (col == 0) rowstart[r] = base;
+      const int c = p % cols, r = p / cols;
+      if (c == 0) rowstart[r] = base;
       const unsigned k = sfi[p];
       if (k == DEB_NOSRC) continue;
-      float4 v = load_bucket(P.buckets, P.bkind, (long long)(WY0 + cr0 + r) * P.W + (WX0 + col));
+      float4 v = load_bucket(P.buckets, P.bkind, (long long)(WY0 + r) * P.W + (WX0 + cc0 + c));
       const float ls = log_scale_nz(v.w, P.k1, P.k2);
+      const unsigned reach = (unsigned)kin[k].w;
       sv[base] = make_float4(v.x * ls, v.y * ls, v.z * ls, v.w * ls);
-      sxyk[base] = (uint32_t)col | ((uint32_t)r << 8) | (k << 16);
+      sxyk[base] = (uint32_t)(cc0 + c) | ((uint32_t)r << 8) | (k << 16) | (reach << 24);
+      atomicMax(rowreach + r, (int)reach);
       base++;
     }
     __syncthreads();
-    /* 4. this warp's band takes every listed source whose kernel reaches it */
-    const int cy = WY0 + cr0; /* absolute row of chunk row 0 */
-    const int rlo = max(0, B0 - R - cy), rhi = min(rows - 1, B0 + DEB_ROWS - 1 + R - cy);
-    if (rlo <= rhi) {
-      const int i1 = rowstart[rhi + 1];
-      for (int i = rowstart[rlo]; i < i1; i++) {
+    /* 4. this warp's band takes every listed source whose kernel reaches it:
+     *    rows whose widest kernel falls short are skipped whole */
+    for (int rr = rlo; rr <= rhi; rr++) {
+      const int sy = WY0 + rr;
+      const int dyb = sy < B0 ? B0 - sy : (sy > B0 + DEB_ROWS - 1 ? sy - (B0 + DEB_ROWS - 1) : 0);
+      if (rowreach[rr] < dyb) continue; /* uniform over the warp */
+      const int i1 = rowstart[rr + 1];
+      for (int i = rowstart[rr]; i < i1; i++) {
         const uint32_t xyk = sxyk[i];
-        const int sx = WX0 + (int)(xyk & 0xffu), sy = cy + (int)((xyk >> 8) & 0xffu);
-        const float4 ki = kin[xyk >> 16];
-        const int reach = (int)ki.w;
+        const int reach = (int)(xyk >> 24);
+        const int sx = WX0 + (int)(xyk & 0xffu);
+        if (reach < dyb || sx + reach < X0 || sx - reach > X0 + DEB_TW - 1) continue; /* uniform */
+        const float4 ki = kin[(xyk >> 16) & 0xffu];
         const int dy0 = B0 - sy;
-        if (dy0 > reach || dy0 + DEB_ROWS - 1 < -reach || sx + reach < X0 || sx - reach > X0 + DEB_TW - 1)
-          continue; /* uniform over the warp */
         const float4 v = sv[i];
         const int r2max = (int)ki.z;
         if (STATS) n_pairs++;
+        /* taps inside the kernel's disc and inside its reach box: the
+         * reference visits offsets up to ceil(h)-1 only (rect.c:121-126),
+         * though an integer width puts non-zero coefficients at distance h;
+         * colf and rowf are zero outside the box */
         const int dx = X0 + lane - sx, dx2 = dx * dx;
-        const float colf = dx2 <= r2max ? exp2f(ki.y * (float)dx2) : 0.0f;
+        const bool xin = dx2 <= r2max && dx >= -reach && dx <= reach;
+        const float colf = xin ? exp2f(ki.y * (float)dx2) : 0.0f;
         const int mdy = dy0 + (lane & (DEB_ROWS - 1));
-        const float rf = ki.x * exp2f(ki.y * (float)(mdy * mdy));
+        const float rf = (mdy >= -reach && mdy <= reach) ? ki.x * exp2f(ki.y * (float)(mdy * mdy)) : 0.0f;
 #pragma unroll
         for (int r = 0; r < DEB_ROWS; r++) {
           const int dy = dy0 + r;
           const float rowf = __shfl_sync(0xffffffffu, rf, r);
-          const bool in = dx2 + dy * dy <= r2max;
-          const float w = in ? colf * rowf : 0.0f;
-          if (STATS) n_taps += __popc(__ballot_sync(0xffffffffu, in));
+          const bool disc = dx2 + dy * dy <= r2max;
+          const float w = disc ? colf * rowf : 0.0f;
+          if (STATS) n_taps += __popc(__ballot_sync(0xffffffffu, disc && xin && dy >= -reach && dy <= reach));
           acc[r][0] = fmaf(w, v.x, acc[r][0]);
           acc[r][1] = fmaf(w, v.y, acc[r][1]);
           acc[r][2] = fmaf(w, v.z, acc[r][2]);
@@ -224,7 +240,7 @@ __global__ void __launch_bounds__(DEB_THREADS) k_de_bands(DEBands P) {
 }
 
 static size_t bands_smem(int nk) {
-  return (size_t)DEB_LCAP * (16 + 4) + (size_t)nk * 16 + DEB_LCAP + (DEB_LCAP / DEB_TW + 2 + DEB_WARPS) * 4;
+  return (size_t)DEB_LCAP * (16 + 4) + (size_t)nk * 16 + DEB_LCAP + (2 * (DEB_WROWS + 1) + DEB_WARPS) * 4;
 }
 
 }  // namespace f3g

@@ -100,6 +100,28 @@ int f3g_launch_fused_log_filter(const void *buckets, int bkind, int W, int H, do
                                 int oversample, const float *filter, int fw, int image_w, int image_h,
                                 unsigned char *out, int earlyclip, const F3GTonemap *tp, cudaStream_t st);
 
+/* Temporal samples planned on the device (f3g_plan.cu).  A key set is the
+ * aligned key genomes of one interpolation segment, laid out from its start
+ * as: this header, nk flam3_genome structs (their scalars and palettes; the
+ * pointers are not used), nk x nx flam3_xform, nk x nstd x nstd chaos
+ * doubles.  Each sample names its key set (byte offset in the key buffer),
+ * the keys' weights and its colour scalar; the kernel fills in the colour
+ * map, xforms, variation lists and choice rows of the sample's pass, whose
+ * other fields the host has uploaded.  d_err[i] != 0: sample i overflowed a
+ * limit (variation lists, choice rows). */
+typedef struct {
+  int nk, nx, nstd, final_index;
+  long long off_genome, off_xform, off_chaos;
+} F3GKeySet;
+typedef struct {
+  long long keyset;
+  double w[4];
+  double color_scalar;
+} F3GPlanSample;
+size_t f3g_plan_smem(int nx, int nstd);
+int f3g_launch_plan(const unsigned char *d_keys, const F3GPlanSample *d_samples, int n, int nx_max, int nstd_max,
+                    F3GPass *d_passes, int *d_err, cudaStream_t st);
+
 /* parity helpers (f3g_probe.cu) */
 int f3g_launch_apply_xform(const F3GPass *d_pass, int fn, int n, const double *d_pin, const uint32_t *d_words,
                            int wpp, double *d_qout, int *d_bad, int precision, cudaStream_t st);

@@ -26,7 +26,9 @@ const char *flam3gpu_last_error(void) { return err_buf; }
 
 const char *flam3gpu_version(void) { return "flam3-gb300 0.1 (sm_103a)"; }
 
-flam3gpu_options f3g_opts = {1, 32, 3, 256, 0, 0, 0, 0, 0, 0, 0, {0}};
+size_t flam3gpu_pass_bytes(void) { return sizeof(F3GPass); }
+
+flam3gpu_options f3g_opts = {1, 32, 3, 256, 0, 0, 0, 0, 0, 0, 0, 0, {0}};
 
 void flam3gpu_default_options(flam3gpu_options *o) {
   memset(o, 0, sizeof(*o));

@@ -48,6 +48,13 @@ int f3g_camera(flam3_frame *spec, const flam3_genome *cp, int field, const f3g_g
 void f3g_pass_key(flam3_frame *spec, uint32_t key[2]);
 unsigned long f3g_irand(randctx *r);
 
+/* pieces of genome interpolation for the device planner (interp.c) */
+int f3g_interp_segment(const flam3_genome *cps, int ncps, double time, int *first, double w[4]);
+void f3g_align_keys(flam3_genome *keys, const flam3_genome *src, int nkeys);
+void f3g_release_genome(flam3_genome *g);
+void f3g_blend_scalars(const flam3_genome *keys, int nk, const double *w, flam3_genome *out);
+int f3g_interp_overridden(void);
+
 /* genome helpers (interp.c) for the XML genome reader (xml.c) */
 void f3g_clear_cp(flam3_genome *cp, int default_flag);
 void f3g_add_xforms(flam3_genome *cp, int num_to_add, int interp_padding, int final_flag);
@@ -109,6 +116,16 @@ typedef struct {
   unsigned long long *d_de_stats; size_t de_stats_bytes;
   double de_work[3];               /* band DE work of the last render (de_stats) */
   float *d_de_c; size_t de_c_bytes;
+  /* device planning of temporal samples: key sets and sample records
+   * (pinned host staging and their device copies), error flags */
+  unsigned char *h_plan_keys; size_t h_plan_keys_bytes;
+  unsigned char *d_plan_keys; size_t d_plan_keys_bytes;
+  F3GPlanSample *h_plan_samples; size_t h_plan_samples_n;
+  F3GPlanSample *d_plan_samples; size_t d_plan_samples_bytes;
+  int *d_plan_err; size_t d_plan_err_bytes;
+  int plan_nx, plan_nstd;
+  /* plan-only probe (flam3gpu_plan_passes): copy batch 0's passes out, skip the render */
+  void *plan_only_out; int plan_only_max, plan_only_n;
   double timings[8];
   /* PNG encoder (png.c): scratch, IDAT chunks, their length, host images */
   void *d_png_work; size_t png_work_bytes;

@@ -718,10 +718,103 @@ static int interpolate_keys(const flam3_genome *cps, int ncps, double time, doub
   return 0;
 }
 
+/* ---- pieces of the blend for the device planner (f3g_plan.cu) ----------- */
+
+/* The keys and weights a temporal sample at `time` blends: the first key of
+ * its segment in cps, the key count (2, or 4 for Catmull-Rom) and the
+ * weights, exactly as interpolate_keys chooses them (stagger 0). */
+int f3g_interp_segment(const flam3_genome *cps, int ncps, double time, int *first, double w[4]) {
+  if (ncps < 2) return -1;
+  int i1 = 0;
+  if (cps[0].time >= time)
+    i1 = 0;
+  else if (cps[ncps - 1].time <= time)
+    i1 = ncps - 2;
+  else
+    while (cps[i1 + 1].time < time) i1++;
+  const int i2 = i1 + 1;
+  double lin0 = (cps[i2].time - time) / (cps[i2].time - cps[i1].time);
+  double lin1 = 1.0 - lin0;
+  if (cps[i1].interpolation != 0 && i1 > 0 && i2 < ncps - 1) {
+    const double t = lin1, t2 = t * t, t3 = t2 * t;
+    w[0] = (2 * t2 - t - t3) / 2;
+    w[1] = (3 * t3 - 5 * t2 + 2) / 2;
+    w[2] = (4 * t2 - 3 * t3 + t) / 2;
+    w[3] = (t3 - t2) / 2;
+    *first = i1 - 1;
+    return 4;
+  }
+  w[0] = lin0;
+  w[1] = lin1;
+  w[2] = w[3] = 0.0;
+  *first = i1;
+  return 2;
+}
+
+void f3g_align_keys(flam3_genome *keys, const flam3_genome *src, int nkeys) { align_keys(keys, src, nkeys); }
+
+void f3g_release_genome(flam3_genome *g) { release(g); }
+
+/* The blended genome without its xforms' variations, parameters, matrices
+ * and palette colours: the scalars, the xforms' densities and opacities, the
+ * chaos rows and the palette's alpha -- what the host needs to size and
+ * check a temporal sample whose genome the device blends.  Same arithmetic
+ * as blend(). */
+void f3g_blend_scalars(const flam3_genome *keys, int nk, const double *w, flam3_genome *out) {
+  const blend_t b = {keys, nk, w};
+  const flam3_genome *k0 = &keys[0];
+  memset(out, 0, sizeof(*out));
+  genome_defaults(out);
+  if (k0->final_xform_index >= 0) {
+    grow_xforms(out, k0->num_xforms - 1, 0, 0);
+    grow_xforms(out, 1, 0, 1);
+  } else {
+    grow_xforms(out, k0->num_xforms, 0, 0);
+  }
+  out->interpolation = 0;
+  out->palette_index = -1;
+  out->spatial_filter_select = k0->spatial_filter_select;
+  out->temporal_filter_type = k0->temporal_filter_type;
+  out->palette_mode = k0->palette_mode;
+  out->interpolation_type = k0->interpolation_type;
+  out->palette_interpolation = k0->palette_interpolation;
+  out->hsv_rgb_palette_blend = k0->hsv_rgb_palette_blend;
+  for (size_t f = 0; f < sizeof(kGenomeDoubles) / sizeof(size_t); f++)
+    *(double *)((char *)out + kGenomeDoubles[f]) = g_sum(&b, kGenomeDoubles[f]);
+  for (size_t f = 0; f < sizeof(kGenomeInts) / sizeof(size_t); f++)
+    *(int *)((char *)out + kGenomeInts[f]) = (int)rint(g_sum_int(&b, kGenomeInts[f]));
+  const int nstd = n_std(k0);
+  for (int i = 0; i < nstd; i++)
+    for (int j = 0; j < nstd; j++) {
+      double v = 0.0;
+      for (int k = 0; k < nk; k++) v += w[k] * keys[k].chaos[i][j];
+      out->chaos[i][j] = v < 0 ? 0 : v;
+    }
+  for (int xf = 0; xf < k0->num_xforms; xf++) {
+    x_block(&b, w, xf, SCALAR_BLOCK_OFF, SCALAR_BLOCK_N, &out->xform[xf]);
+    if (out->xform[xf].density < 0.0) out->xform[xf].density = 0.0;
+  }
+  for (int i = 0; i < 256; i++) {
+    double alpha = 0.0;
+    int opaque = 1;
+    if (k0->palette_interpolation == 1) {
+      out->palette[i].color[3] = keys[(i < (256 * w[0])) ? 0 : 1].palette[i].color[3];
+      continue;
+    }
+    for (int k = 0; k < nk; k++) {
+      alpha += w[k] * keys[k].palette[i].color[3];
+      opaque &= keys[k].palette[i].color[3] == 1.0;
+    }
+    out->palette[i].color[3] = clamp01(opaque ? 1.0 : alpha);
+  }
+}
+
 /* optional override: the reference's flam3_interpolate, when the caller links it */
 static void (*g_interp)(flam3_genome *, int, double, double, flam3_genome *) = NULL;
 
 void flam3gpu_set_interpolator(void (*fn)(flam3_genome *, int, double, double, flam3_genome *)) { g_interp = fn; }
+
+int f3g_interp_overridden(void) { return g_interp != NULL; }
 
 int f3g_interpolate_n(flam3_genome *cps, int ncps, double time, flam3_genome *result) {
   if (g_interp) {

@@ -402,6 +402,213 @@ int f3g_build_batch_passes(flam3_frame *spec, int field, const f3g_geom *g, int 
   return 0;
 }
 
+/* ---- temporal samples planned on the device (f3g_plan.cu) ----
+ * For frames with several genomes the host does only what it needs before
+ * the launch: each sample's key segment and weights (the keys of a segment
+ * aligned once), the genome scalars, xform weights, chaos rows and palette
+ * alpha of its blend (camera, sample count, choice mode, checks) and the
+ * pass header.  The key sets and one record per sample are staged in pinned
+ * memory for the plan kernel, which fills in the colour map, xforms,
+ * variation lists and choice rows on the device. */
+typedef struct {
+  int first, n;
+  size_t off;
+  flam3_genome keys[4];
+} plan_seg;
+
+static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+static int plan_stage_keys(f3g_ctx *c, size_t need, size_t keep) {
+  if (need <= c->h_plan_keys_bytes) return 0;
+  size_t cap = need < 65536 ? 65536 : 2 * need;
+  unsigned char *nb = NULL;
+  if (cudaMallocHost((void **)&nb, cap) != cudaSuccess) {
+    f3g_set_error("cudaMallocHost of %zu bytes failed", cap);
+    return 1;
+  }
+  if (c->h_plan_keys) {
+    memcpy(nb, c->h_plan_keys, keep);
+    cudaFreeHost(c->h_plan_keys);
+  }
+  c->h_plan_keys = nb;
+  c->h_plan_keys_bytes = cap;
+  return 0;
+}
+
+/* Returns 0 with the batch planned for the device, 1 on error, -1 when the
+ * frame needs the host planner (lists beyond the pass's capacity). */
+static int build_batch_passes_device(f3g_ctx *c, flam3_frame *spec, int field, const f3g_geom *g, int batch,
+                                     int nbatches, int ntemporal, const double *tfilter, const double *tdeltas,
+                                     int cmap_size, F3GPass *passes, f3g_pass_info *info, size_t *key_bytes) {
+  /* a frame whose keys could make more active variations than a pass holds
+   * stays on the host planner (which reports the limit) */
+  for (int k = 0; k < spec->ngenomes; k++) {
+    const flam3_genome *gk = &spec->genomes[k];
+    if (gk->num_xforms > F3G_MAX_XFORMS) return -1;
+  }
+  {
+    int nv = 0, nxm = 0;
+    for (int k = 0; k < spec->ngenomes; k++) nxm = spec->genomes[k].num_xforms > nxm ? spec->genomes[k].num_xforms : nxm;
+    for (int xf = 0; xf < nxm; xf++)
+      for (int j = 0; j < flam3_nvariations; j++) {
+        int any = j == 0; /* padding xforms may take linear */
+        for (int k = 0; k < spec->ngenomes && !any; k++)
+          if (xf < spec->genomes[k].num_xforms && spec->genomes[k].xform[xf].var[j] != 0) any = 1;
+        nv += any;
+      }
+    if (nv + 8 * nxm > F3G_MAX_VARLIST) return -1;
+  }
+  if (c->h_plan_samples_n < (size_t)ntemporal) {
+    if (c->h_plan_samples) cudaFreeHost(c->h_plan_samples);
+    c->h_plan_samples = NULL;
+    c->h_plan_samples_n = 0;
+    if (cudaMallocHost((void **)&c->h_plan_samples, (size_t)ntemporal * sizeof(F3GPlanSample)) != cudaSuccess) {
+      f3g_set_error("cudaMallocHost of the plan records failed");
+      return 1;
+    }
+    c->h_plan_samples_n = (size_t)ntemporal;
+  }
+  /* keys in order: the caller's ISAAC context advances as the reference's */
+  for (int ts = 0; ts < ntemporal; ts++) consume_rc(spec, passes[ts].key);
+  plan_seg *segs = (plan_seg *)calloc((size_t)ntemporal, sizeof(plan_seg));
+  int nseg = 0, rc = 1;
+  size_t used = 0;
+  flam3_genome sg;
+  memset(&sg, 0, sizeof(sg));
+  c->plan_nx = c->plan_nstd = 0;
+  for (int ts = 0; ts < ntemporal; ts++) {
+    const int gi = batch * ntemporal + ts;
+    const double tst = spec->time + tdeltas[gi];
+    double w[4];
+    int first = 0;
+    const int n = f3g_interp_segment(spec->genomes, spec->ngenomes, tst, &first, w);
+    int si = -1;
+    for (int k = 0; k < nseg; k++)
+      if (segs[k].first == first && segs[k].n == n) si = k;
+    if (si < 0) {
+      plan_seg *sp = &segs[nseg];
+      sp->first = first;
+      sp->n = n;
+      f3g_align_keys(sp->keys, &spec->genomes[first], n);
+      const int nx = sp->keys[0].num_xforms, nstd = nx - (sp->keys[0].final_xform_index >= 0);
+      F3GKeySet ks;
+      ks.nk = n;
+      ks.nx = nx;
+      ks.nstd = nstd;
+      ks.final_index = sp->keys[0].final_xform_index;
+      ks.off_genome = (long long)align16(sizeof(F3GKeySet));
+      ks.off_xform = (long long)align16((size_t)ks.off_genome + (size_t)n * sizeof(flam3_genome));
+      ks.off_chaos = (long long)align16((size_t)ks.off_xform + (size_t)n * nx * sizeof(flam3_xform));
+      const size_t off = align16(used), total = (size_t)ks.off_chaos + (size_t)n * nstd * nstd * sizeof(double);
+      if (plan_stage_keys(c, off + total, used)) goto out;
+      unsigned char *b = c->h_plan_keys + off;
+      memcpy(b, &ks, sizeof(ks));
+      for (int k = 0; k < n; k++) {
+        memcpy(b + ks.off_genome + (size_t)k * sizeof(flam3_genome), &sp->keys[k], sizeof(flam3_genome));
+        memcpy(b + ks.off_xform + (size_t)k * nx * sizeof(flam3_xform), sp->keys[k].xform, (size_t)nx * sizeof(flam3_xform));
+        for (int i = 0; i < nstd; i++)
+          memcpy(b + ks.off_chaos + ((size_t)k * nstd + i) * nstd * sizeof(double), sp->keys[k].chaos[i],
+                 (size_t)nstd * sizeof(double));
+      }
+      sp->off = off;
+      used = off + total;
+      if (nx > c->plan_nx) c->plan_nx = nx;
+      if (nstd > c->plan_nstd) c->plan_nstd = nstd;
+      si = nseg++;
+    }
+    plan_seg *sp = &segs[si];
+    F3GPlanSample *rec = &c->h_plan_samples[ts];
+    rec->keyset = (long long)sp->off;
+    for (int k = 0; k < 4; k++) rec->w[k] = w[k];
+    rec->color_scalar = tfilter[gi];
+    /* the blend's scalars, xform weights, chaos rows and palette alpha */
+    f3g_release_genome(&sg);
+    f3g_blend_scalars(sp->keys, n, w, &sg);
+    const int nx = sg.num_xforms, nstd = nx - (sg.final_xform_index >= 0);
+    F3GPass *p = &passes[ts];
+    f3g_pass_info *in = &info[ts];
+    const uint32_t key0 = p->key[0], key1 = p->key[1];
+    memset(p, 0, offsetof(F3GPass, xf));
+    p->key[0] = key0;
+    p->key[1] = key1;
+    memset(in, 0, sizeof(*in));
+    int unity = 1;
+    for (int i = 0; i < nstd; i++)
+      for (int j = 0; j < nstd; j++)
+        if (fabs(sg.chaos[i][j] - 1.0) > F3G_EPS) unity = 0;
+    /* choice rows of zero total weight (flam3.c:190-196) */
+    for (int r = -1; r < (unity ? 0 : nstd); r++) {
+      double dr = 0.0;
+      for (int i = 0; i < nstd; i++) dr += r >= 0 ? sg.xform[i].density * sg.chaos[r][i] : sg.xform[i].density;
+      if (dr == 0.0) {
+        f3g_set_error("cannot iterate empty flame.");
+        goto out;
+      }
+    }
+    p->num_xforms = nx;
+    p->num_std = nstd;
+    p->final_index = sg.final_xform_index;
+    p->final_enable = sg.final_xform_enable == 1 && sg.final_xform_index >= 0;
+    p->chaos_enable = 1 - unity;
+    p->cmap_size = cmap_size;
+    p->palette_mode = sg.palette_mode;
+    /* the iterate kernel's instantiation: extended variations in any key */
+    for (int k = 0; k < n && !p->full_variations; k++)
+      for (int xf = 0; xf < nx && !p->full_variations; xf++)
+        for (int j = 20; j < flam3_nvariations; j++)
+          if (sp->keys[k].xform[xf].var[j] != 0) {
+            p->full_variations = 1;
+            break;
+          }
+    if (set_camera(spec, &sg, field, g, p, &in->sample_density, &in->ppux, &in->ppuy)) goto out;
+    const double nsamples = in->sample_density * g->image_width * g->image_height;
+    in->batch_size = nsamples / (nbatches * ntemporal);
+    p->samples = (long long)in->batch_size;
+    p->fuse = spec->earlyclip ? 100 : 15;
+    p->iter_mode = (p->chaos_enable || f3g_opts.iter_mode == 0) ? 0 : 1;
+    for (int j = 0; j < 256; j++)
+      if (sg.palette[j].color[3] != 1.0) in->need_count = 1;
+    in->vibrancy = sg.vibrancy;
+    in->gamma = sg.gamma;
+    for (int k = 0; k < 3; k++) in->background[k] = sg.background[k];
+    in->contrast = sg.contrast;
+    in->brightness = sg.brightness;
+    in->gam_lin_thresh = sg.gam_lin_thresh;
+    in->estimator_curve = sg.estimator_curve;
+  }
+  *key_bytes = used;
+  rc = 0;
+out:
+  f3g_release_genome(&sg);
+  for (int k = 0; k < nseg; k++)
+    for (int i = 0; i < segs[k].n; i++) f3g_release_genome(&segs[k].keys[i]);
+  free(segs);
+  return rc;
+}
+
+/* Uploads the staged key sets and sample records and launches the plan
+ * kernel over the passes (whose headers are already on the device). */
+static int launch_device_plan(f3g_ctx *c, int ntemporal, size_t key_bytes) {
+  if (f3g_ensure((void **)&c->d_plan_keys, &c->d_plan_keys_bytes, key_bytes) ||
+      f3g_ensure((void **)&c->d_plan_samples, &c->d_plan_samples_bytes, (size_t)ntemporal * sizeof(F3GPlanSample)) ||
+      f3g_ensure((void **)&c->d_plan_err, &c->d_plan_err_bytes, (size_t)ntemporal * sizeof(int)))
+    return 1;
+  if (cudaMemcpyAsync(c->d_plan_keys, c->h_plan_keys, key_bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+      cudaMemcpyAsync(c->d_plan_samples, c->h_plan_samples, (size_t)ntemporal * sizeof(F3GPlanSample),
+                      cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->d_plan_err, 0, (size_t)ntemporal * sizeof(int), c->stream) != cudaSuccess) {
+    f3g_set_error("plan upload failed");
+    return 1;
+  }
+  int e = f3g_launch_plan(c->d_plan_keys, c->d_plan_samples, ntemporal, c->plan_nx, c->plan_nstd, c->d_passes,
+                          c->d_plan_err, c->stream);
+  if (e) {
+    f3g_set_error("plan launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    return 1;
+  }
+  return 0;
+}
+
 /* Copies n values as floats to a device buffer through the context's pinned
  * staging area at float offset `slot` (so the copy is truly asynchronous);
  * a slot may be reused only after the stream has passed the copy. */
@@ -592,10 +799,19 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
       if (f3g_ensure(&c->d_count, &c->count_bytes, (size_t)nb * csz)) goto done;
       CK(cudaMemsetAsync(c->d_count, 0, (size_t)nb * csz, c->stream));
     }
-    /* ---- passes of this batch ---- */
+    /* ---- passes of this batch: multi-genome frames planned on the device ---- */
     long long total_chunks = 0, batch_samples = 0;
-    if (f3g_build_batch_passes(spec, field, &g, batch, nbatches, ntemporal, tfilter, tdeltas, cmap_size, c->h_passes,
-                               c->h_info))
+    int dev_plan = 0;
+    size_t key_bytes = 0;
+    if (spec->ngenomes > 1 && !f3g_opts.host_plan && !f3g_interp_overridden()) {
+      if (batch > 0) CK(cudaStreamSynchronize(c->stream)); /* the staging of the previous batch is read */
+      const int r = build_batch_passes_device(c, spec, field, &g, batch, nbatches, ntemporal, tfilter, tdeltas,
+                                              cmap_size, c->h_passes, c->h_info, &key_bytes);
+      if (r > 0) goto done;
+      dev_plan = r == 0;
+    }
+    if (!dev_plan && f3g_build_batch_passes(spec, field, &g, batch, nbatches, ntemporal, tfilter, tdeltas, cmap_size,
+                                            c->h_passes, c->h_info))
       goto done;
     for (int ts = 0; ts < ntemporal; ts++) {
       F3GPass *p = &c->h_passes[ts];
@@ -656,15 +872,31 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
       int nxmax = 0;
       for (int ts = 0; ts < ntemporal; ts++)
         if (c->h_passes[ts].num_xforms > nxmax) nxmax = c->h_passes[ts].num_xforms;
-      const size_t pass_bytes = F3G_PASS_BYTES(nxmax);
+      /* device-planned passes: the headers here, the rest from the plan kernel */
+      const size_t pass_bytes = dev_plan ? offsetof(F3GPass, xf) : F3G_PASS_BYTES(nxmax);
       CK(cudaMemcpy2DAsync(c->d_passes, sizeof(F3GPass), c->h_passes, sizeof(F3GPass), pass_bytes,
                            (size_t)ntemporal, cudaMemcpyHostToDevice, c->stream));
+      if (dev_plan) {
+        if (launch_device_plan(c, ntemporal, key_bytes)) goto done;
+        launches++;
+        h2d += (double)key_bytes + (double)ntemporal * sizeof(F3GPlanSample);
+      }
       h2d += (double)ntemporal * pass_bytes + (double)(ntemporal + 1) * sizeof(long long) +
              (double)ntemporal * sizeof(F3GItem);
       CK(cudaMemcpyAsync(c->d_prefix, c->h_prefix, (size_t)(ntemporal + 1) * sizeof(long long),
                                cudaMemcpyHostToDevice, c->stream));
       CK(cudaMemcpyAsync(c->d_items, c->h_items, (size_t)ntemporal * sizeof(F3GItem), cudaMemcpyHostToDevice,
                          c->stream));
+      if (c->plan_only_out) {
+        /* plan-only probe: batch 0's passes to the caller, no render */
+        const int n = ntemporal < c->plan_only_max ? ntemporal : c->plan_only_max;
+        CK(cudaMemcpyAsync(c->plan_only_out, c->d_passes, (size_t)n * sizeof(F3GPass), cudaMemcpyDeviceToHost,
+                           c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->plan_only_n = n;
+        rv = 0;
+        goto done;
+      }
       int shuffle = f3g_opts.shuffle_every > 0 ? f3g_opts.shuffle_every : 1;
       /* rounds: one launch, or ~10 launches with progress callbacks between */
       int nrounds = spec->progress ? 10 : 1;
@@ -997,6 +1229,24 @@ double flam3gpu_render_memory_required(flam3_frame *f) {
   int bsz = f->bits == 64 ? 32 : 16;
   double nb = (double)cp->spatial_oversample * cp->spatial_oversample * (double)cp->width * cp->height;
   return nb * bsz * 2.0 + (double)cp->width * cp->height * 4 * 2;
+}
+
+int flam3gpu_plan_passes(flam3_frame *f, int on_device, void *passes, int max_passes) {
+  f3g_ctx *c = f3g_get_ctx();
+  if (!c) {
+    f3g_set_error("no CUDA device available");
+    return -1;
+  }
+  const flam3gpu_options saved = f3g_opts;
+  f3g_opts.host_plan = !on_device;
+  c->plan_only_out = passes;
+  c->plan_only_max = max_passes;
+  c->plan_only_n = 0;
+  stat_struct st;
+  const int r = flam3gpu_render_ex(f, NULL, 0, 3, 0, &st, NULL);
+  c->plan_only_out = NULL;
+  f3g_opts = saved;
+  return r ? -1 : c->plan_only_n;
 }
 
 int flam3gpu_last_de_work(double w[3]) {

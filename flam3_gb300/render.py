@@ -33,7 +33,8 @@ class Options(C.Structure):
     _fields_ = [("iter_mode", C.c_int), ("iter_precision", C.c_int), ("shuffle_every", C.c_int),
                 ("threads_per_block", C.c_int), ("blocks", C.c_int), ("chain_samples", C.c_int),
                 ("seed_salt", C.c_uint64), ("de_tile", C.c_int), ("de_kernel", C.c_int),
-                ("de_stats", C.c_int), ("float_buckets", C.c_int), ("reserved", C.c_int * 4)]
+                ("de_stats", C.c_int), ("float_buckets", C.c_int), ("host_plan", C.c_int),
+                ("reserved", C.c_int * 3)]
 
 
 class PngText(C.Structure):
@@ -77,6 +78,8 @@ def load():
     lib.flam3gpu_iterate_chains.argtypes = [G, C.c_int, C.c_int, C.c_int, dp, C.c_uint64, dp,
                                             C.POINTER(C.c_long), C.c_int]
     lib.flam3gpu_xform_choice_table.argtypes = [G, C.POINTER(C.c_uint16), C.POINTER(C.c_int)]
+    lib.flam3gpu_plan_passes.argtypes = [F, C.c_int, C.c_void_p, C.c_int]
+    lib.flam3gpu_pass_bytes.restype = C.c_size_t
     lib.flam3gpu_interpolate.argtypes = [G, C.c_int, C.c_double, C.c_double, G]
     lib.flam3gpu_estimate_bounding_box.argtypes = [G, C.c_double, C.c_int, dp, dp, C.POINTER(abi.randctx)]
     lib.flam3gpu_colorhist.argtypes = [G, C.c_int, C.POINTER(abi.randctx), dp]
@@ -250,6 +253,19 @@ def xform_choice_table(genome):
     if lib.flam3gpu_xform_choice_table(C.byref(g), out.ctypes.data_as(C.POINTER(C.c_uint16)), C.byref(rows)):
         _err(lib, "flam3gpu_xform_choice_table")
     return out[:rows.value * 16384].reshape(rows.value, 16384)
+
+
+def plan_passes(frame, on_device, max_passes=1024):
+    """The first batch's passes of `frame` as flam3gpu_render plans them, on
+    the device or on host threads: raw records of flam3gpu_pass_bytes() each
+    (a uint8 array of shape (n, bytes))."""
+    lib = load()
+    size = lib.flam3gpu_pass_bytes()
+    buf = np.zeros(max_passes * size, np.uint8)
+    n = lib.flam3gpu_plan_passes(C.byref(frame.f), 1 if on_device else 0, buf.ctypes.data, max_passes)
+    if n < 0:
+        _err(lib, "flam3gpu_plan_passes")
+    return buf[:n * size].reshape(n, size)
 
 
 def accumulate_points(frame, points, field=0):

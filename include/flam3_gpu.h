@@ -339,7 +339,11 @@ const char *flam3gpu_version(void);
  * float_buckets: 0 = the reference's integer arithmetic for bits 32 and 33
  * (each hit's channels truncated before the add, and for bits 32 the
  * log-scaled accumulator truncated too, flam3.c:3642-3647, 3688-3703,
- * 3771-3856); 1 = exact FP32 sums (more accurate than the reference). */
+ * 3771-3856); 1 = exact FP32 sums (more accurate than the reference).
+ * host_plan: 0 = the temporal samples of frames with several genomes
+ * (animation, motion blur) are interpolated, prepared and packed on the
+ * device, one block per sample; 1 = on host threads (always for one genome,
+ * and when a caller interpolator is installed). */
 typedef struct {
   int iter_mode;
   int iter_precision;
@@ -352,7 +356,8 @@ typedef struct {
   int de_kernel;      /* 0 owner bands (default), 1 fused tile */
   int de_stats;       /* 1: band DE counts its work (flam3gpu_last_de_work) */
   int float_buckets;  /* 1: bits 32/33 keep exact FP32 sums (no per-hit truncation) */
-  int reserved[4];
+  int host_plan;      /* 1: plan every temporal sample on host threads (0: multi-genome frames on the device) */
+  int reserved[3];
 } flam3gpu_options;
 
 void flam3gpu_default_options(flam3gpu_options *o);

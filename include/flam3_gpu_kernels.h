@@ -64,6 +64,18 @@ int flam3gpu_apply_xform(flam3_genome *cp, int fn, int n, const double *p_in,
  * entries and receives the row count in *rows. */
 int flam3gpu_xform_choice_table(flam3_genome *cp, uint16_t *table, int *rows);
 
+/* The passes (per temporal sample: interpolated genome, prepared xforms,
+ * choice rows, colour map, camera) that flam3gpu_render would build for the
+ * first batch of frame f, planned on the device (on_device = 1) or on host
+ * threads (0), copied to `passes` as sizeof(F3GPass) records (at most
+ * max_passes); nothing is rendered and f->rc advances as a render's would.
+ * No counterpart in the reference: the parity probe of the device planner
+ * against the host's restatement of flam3_interpolate (flam3.c:717-802) and
+ * rect.c:754-827.  Returns the number of passes, -1 on failure. */
+int flam3gpu_plan_passes(flam3_frame *f, int on_device, void *passes, int max_passes);
+/* sizeof the pass record flam3gpu_plan_passes writes */
+size_t flam3gpu_pass_bytes(void);
+
 /* GPU bucket accumulation (rect.c:411-516) of a host point stream
  * (n x 4 doubles) for genome f->genomes[0] at f->time; adds into a host FP64
  * 5-channel histogram of the render's geometry.  bits selects the device

@@ -112,8 +112,9 @@ int flam3gpu_render_batch(flam3_frame *frames, int n, void **outs, int field, in
  * oversample, estimator radius) in the process-wide table, and returns the
  * number of classes tuned:
  *   chains per job  -- samples per chain (the chunk length) S in {128 .. 1024};
- *   DE tile shape   -- output-tile edge of the fused density-estimation
- *                      kernel in {8, 16, 32}.
+ *   DE tile shape   -- density estimation by owner bands (32 x 64 bucket
+ *                      tiles) or the fused density-estimation kernel with
+ *                      an output-tile edge in {8, 16, 32}.
  * Services created with use_tuning apply the table to new jobs. */
 int flam3gpu_autotune(flam3_frame *frames, int n, double quality_scale);
 /* Writes / reads the table as text ("key S tile" per line). */
