@@ -1243,7 +1243,8 @@ int flam3gpu_plan_passes(flam3_frame *f, int on_device, void *passes, int max_pa
   c->plan_only_max = max_passes;
   c->plan_only_n = 0;
   stat_struct st;
-  const int r = flam3gpu_render_ex(f, NULL, 0, 3, 0, &st, NULL);
+  unsigned char unused; /* the render stops after planning: the image buffer is never written */
+  const int r = flam3gpu_render_ex(f, &unused, 0, 3, 0, &st, NULL);
   c->plan_only_out = NULL;
   f3g_opts = saved;
   return r ? -1 : c->plan_only_n;
