@@ -71,6 +71,7 @@ typedef struct f3g_job {
   long long nb;
   int nbatches, ntemporal, threads, precision;
   int fused_de, fused_log, need_acc, count_any, tile, band_de;
+  int aborted; /* the progress callback asked to abort: no more rounds, no tail, output untouched */
   F3GPass *h_passes;      /* nbatches * ntemporal */
   long long *pass_prefix; /* per batch: ntemporal+1 chunk offsets, concatenated */
   batch_plan *bp;
@@ -141,6 +142,7 @@ struct flam3gpu_service {
   size_t budget, used, peak;
   round_buf rb[NRB];
   unsigned long long round_no;
+  int paused; /* jobs the last round left out because their progress callback paused them */
   int inflight[NRB];
   tail_slot ts[NTAIL];
   unsigned long long tail_no;
@@ -952,6 +954,7 @@ static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n) {
     /* one graph per job tail, keyed by its shape; the executable graph of a
      * shape is updated in place with the next job's buffers and sizes */
     for (int i = 0; i < n && !err; i++) {
+      if (jobs[i]->aborted) continue; /* an aborted job has no tail */
       char sig[128];
       sig[0] = 0;
       cudaGraph_t graph = NULL;
@@ -978,6 +981,7 @@ static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n) {
       cudaEventRecord(s->ev_fork, s->s_tail);
       int used[NBRANCH] = {0};
       for (int i = 0; i < n && !err; i++) {
+        if (jobs[i]->aborted) continue;
         const int k = i % s->cfg.tail_branches;
         if (!used[k]) {
           cudaStreamWaitEvent(s->s_br[k], s->ev_fork, 0);
@@ -1002,7 +1006,8 @@ static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n) {
     }
     if (graph) cudaGraphDestroy(graph);
   } else {
-    for (int i = 0; i < n && !err; i++) err = enqueue_tail_ops(s, jobs[i], s->s_tail, NULL, 0);
+    for (int i = 0; i < n && !err; i++)
+      if (!jobs[i]->aborted) err = enqueue_tail_ops(s, jobs[i], s->s_tail, NULL, 0);
   }
   if (err) {
     const char *m = cudaGetErrorString(cudaGetLastError());
@@ -1028,6 +1033,12 @@ static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n) {
  * interleaved for fields) and returns the staging buffer */
 static void copy_out(f3g_job *j) {
   if (!j->h_out) return;
+  if (j->aborted) { /* the reference leaves the output as it stands (rect.c:919-922) */
+    pin_put(j->h_out, align256(j->out_bytes) + 2 * sizeof(unsigned long long));
+    j->h_out = NULL;
+    j->h_counts = NULL;
+    return;
+  }
   const f3g_geom *g = &j->g;
   const size_t row = (size_t)g->image_width * j->nchan * j->spec.bytes_per_channel;
   unsigned char *dst = (unsigned char *)j->out;
@@ -1139,11 +1150,27 @@ static int issue_round(flam3gpu_service *s) {
   f3g_job **tails = (f3g_job **)malloc((size_t)(na + 1) * sizeof(f3g_job *));
   long long *takes = (long long *)malloc((size_t)(na + 1) * sizeof(long long));
   int nc = 0, ntails = 0;
+  s->paused = 0;
   for (int i = 0; i < na; i++) {
     f3g_job *j = s->active[i];
     if (j->phase != P_ITER) continue;
+    /* the request's progress callback, between the rounds of its job
+     * (rect.c:324-391: 1 aborts, 2 pauses); called on the service thread */
+    if (j->spec.progress && !j->aborted) {
+      const double pct = j->total_samples > 0 ? 100.0 * j->done_samples / j->total_samples : 0.0;
+      const int r = j->spec.progress(j->spec.progress_parameter, pct, 0, 0.0);
+      if (r == 1) {
+        j->aborted = 1;
+        j->batch = j->nbatches - 1;
+        j->cursor = j->bp[j->batch].chunks;
+        if (j->h_counts) j->h_counts[0] = j->h_counts[1] = 0;
+      } else if (r == 2) {
+        s->paused++;
+        continue;
+      }
+    }
     if (j->cursor < j->bp[j->batch].chunks) cand[nc++] = j;
-    else tails[ntails++] = j; /* a batch without samples goes straight to its tail */
+    else tails[ntails++] = j; /* a batch without samples (or an aborted job) goes straight to its tail */
   }
   if (!nc) {
     if (ntails) enqueue_tails(s, tails, ntails);
@@ -1421,6 +1448,7 @@ static void *service_main(void *arg) {
     const int issued = issue_round(s);
     s->h_round += now_s() - t0;
     if (issued) continue;
+    const int paused = s->paused;
     /* nothing to issue: wait for the GPU, or for submissions */
     t0 = now_s();
     const int busy = poll_tails(s);
@@ -1444,11 +1472,12 @@ static void *service_main(void *arg) {
         break;
       }
       pthread_cond_wait(&s->cv_work, &s->mu);
-    } else if (s->nactive == 0 || s->pend_head) {
-      /* queued work that does not fit yet, or a retry after a pool miss */
+    } else if (s->nactive == 0 || s->pend_head || paused) {
+      /* queued work that does not fit yet, a retry after a pool miss, or
+       * paused jobs to ask again (every 10 ms) */
       struct timespec dl;
       clock_gettime(CLOCK_REALTIME, &dl);
-      dl.tv_nsec += 1000000;
+      dl.tv_nsec += paused ? 10000000 : 1000000;
       if (dl.tv_nsec >= 1000000000) {
         dl.tv_sec++;
         dl.tv_nsec -= 1000000000;

@@ -65,7 +65,14 @@ flam3gpu_service *flam3gpu_service_create(const flam3gpu_service_config *cfg);
 /* Queues one render with flam3_render's arguments.  The frame and its
  * genomes are copied (the caller may reuse them at once) and f->rc is
  * advanced now, exactly as flam3_render would advance it.  `out` must stay
- * valid until the job completes.  *ticket identifies the job. */
+ * valid until the job completes.  *ticket identifies the job.  A frame's
+ * progress callback (f->progress, f->progress_parameter) is called on the
+ * service thread before each iterate round the job could take part in, with
+ * the percentage of its samples done and stage 0: returning 1 aborts the
+ * job (no further rounds and no filtering; it completes with 0 and leaves
+ * `out` as it stands, as flam3_render's abort does, rect.c:919-922),
+ * returning 2 pauses it (it is left out of rounds and asked again about
+ * every 10 ms). */
 int flam3gpu_service_submit(flam3gpu_service *s, flam3_frame *f, void *out, int field, int nchan, int transp,
                             uint64_t *ticket);
 

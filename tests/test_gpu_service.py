@@ -12,7 +12,7 @@ import threading
 import numpy as np
 import pytest
 
-from flam3_gb300 import genome as gm, render, service
+from flam3_gb300 import abi, genome as gm, render, service
 
 pytestmark = pytest.mark.gpu
 
@@ -216,3 +216,46 @@ def test_autotune_table_roundtrip(gpulib, tmp_path):
     finally:
         service.autotune_clear()
     assert float(np.mean(np.abs(out.astype(float) - ref.astype(float)))) < 3.0
+
+
+def test_progress_callback_abort_pause_and_batch(gpulib):
+    """Requests with a progress callback (the contract of rect.c:324-391):
+    one that aborts at its first call completes with its output untouched
+    while the requests beside it render; one that pauses for its first three
+    calls renders after it resumes, like the plain render; the batch API calls
+    the callbacks too."""
+    calls = {"abort": [], "pause": [], "batch": []}
+
+    def callback(name, answer):
+        @abi.PROGRESS_FN
+        def f(param, pct, stage, eta):
+            calls[name].append(pct)
+            return answer(len(calls[name]))
+        return f
+
+    abort_cb = callback("abort", lambda n: 1)
+    pause_cb = callback("pause", lambda n: 2 if n <= 3 else 0)
+    Fa, Fp, Fo = frame("de", 1), frame("de", 2), frame("plain", 3)
+    Fa.f.progress = abort_cb
+    Fp.f.progress = pause_cb
+    with service.Service(round_samples=1 << 20) as svc:
+        ta, tp, to = svc.submit(Fa), svc.submit(Fp), svc.submit(Fo)
+        out_a, _, _ = svc.wait(ta)
+        out_p, st_p, _ = svc.wait(tp)
+        out_o, _, _ = svc.wait(to)
+        cnt = svc.counters()
+    assert len(calls["abort"]) == 1 and not out_a.any()
+    assert len(calls["pause"]) >= 4 and all(0.0 <= c <= 100.0 for c in calls["pause"])
+    ref_p, st_ref, _ = plain("de", 2)
+    ok, info = close_images(out_p, ref_p)
+    assert ok, info
+    assert st_p.num_iters == st_ref.num_iters
+    ref_o, _, _ = plain("plain", 3)
+    ok, info = close_images(out_o, ref_o)
+    assert ok, info
+    assert cnt["jobs_done"] == 3 and cnt["jobs_failed"] == 0
+    batch_cb = callback("batch", lambda n: 0)
+    Fb = frame("de", 0)
+    Fb.f.progress = batch_cb
+    (out_b, _), = service.render_batch([Fb])
+    assert len(calls["batch"]) >= 1 and out_b.mean() > 1.0
