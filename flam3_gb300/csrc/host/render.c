@@ -136,6 +136,10 @@ static int compute_geom(flam3_frame *spec, const flam3_genome *cp, int field, do
     g->out_width *= 2;
   } else
     g->image_height = cp->height;
+  if (g->image_width < 1 || g->image_height < 1) {
+    f3g_set_error("image size must be positive, not %dx%d.", g->image_width, g->image_height);
+    return 1;
+  }
   double *flt = NULL;
   g->filter_width = f3g_spatial_filter(spec, field, &flt);
   if (g->filter_width < 0) return 1;
