@@ -643,8 +643,7 @@ int flam3gpu_service_submit(flam3gpu_service *s, flam3_frame *f, void *out, int 
     return 1;
   }
   j->t_submit = now_s();
-  j->spec = *f;
-  j->spec.progress = NULL;
+  j->spec = *f; /* keeps the request's progress callback, called between rounds */
   j->spec.genomes = (flam3_genome *)calloc((size_t)f->ngenomes, sizeof(flam3_genome));
   for (int i = 0; i < f->ngenomes; i++) f3g_genome_copy(&j->spec.genomes[i], &f->genomes[i]);
   j->out = out;
@@ -949,7 +948,8 @@ static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n) {
   }
   for (int k = 0; k < s->cfg.streams; k++) cudaStreamWaitEvent(s->s_tail, s->ev_last[k], 0);
   cudaEventRecord(t->t0, s->s_tail);
-  int err = 0;
+  int err = 0, live = 0;
+  for (int i = 0; i < n; i++) live += !jobs[i]->aborted;
   if (s->cfg.tail_graphs == 1) {
     /* one graph per job tail, keyed by its shape; the executable graph of a
      * shape is updated in place with the next job's buffers and sizes */
@@ -971,7 +971,7 @@ static void enqueue_tails_impl(flam3gpu_service *s, f3g_job **jobs, int n) {
       }
       if (graph) cudaGraphDestroy(graph);
     }
-  } else if (s->cfg.tail_graphs == 2) {
+  } else if (s->cfg.tail_graphs == 2 && live) {
     /* one graph per round, one branch per job across tail_branches streams */
     char sig[512];
     sig[0] = 0;
