@@ -15,11 +15,8 @@
  * reads the work counters back to the host between the iteration and the
  * tail, so the call returns only when the image is in the caller's buffer.
  *
- * Set-up: the first call on each device looks up the array's device address
- * with cudaGetSymbolAddress (with that device current) and keeps it for the
- * rest of the process; make that first call before any stream capture.  A
- * cudaDeviceReset unloads the module and may move the array, so the entry
- * point must not be used on a device after that device was reset.
+ * Each call looks up the array's address on the current device with
+ * cudaGetSymbolAddress.
  *
  * Limits: one batch (nbatches == 1), and the render's scratch must fit the
  * array; larger requests are refused with an error naming both sizes.
@@ -34,8 +31,6 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include <mutex>
-
 #include "f3g_launch.h"
 #include "host/f3g_host.h"
 
@@ -45,31 +40,19 @@
 
 static __device__ __align__(256) unsigned char f3g_noalloc_scratch[F3G_NOALLOC_BYTES];
 
-#define F3G_MAX_DEVICES 64
-
-/* The array's device address, looked up once per device with that device
- * current.  In host code `f3g_noalloc_scratch` names a host-side stand-in,
- * not device memory, so only this address is ever passed to kernels. */
+/* The array's device address on the current device, looked up on every
+ * call (the lookup is cheap, and a reset device may place the array
+ * elsewhere).  In host code `f3g_noalloc_scratch` names a host-side
+ * stand-in, not device memory, so only this address is ever passed to
+ * kernels. */
 static int scratch_address(unsigned char **out) {
-  static std::mutex mu;
-  static unsigned char *addr[F3G_MAX_DEVICES];
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= F3G_MAX_DEVICES) {
-    f3g_set_error("no usable CUDA device for the no-allocation render");
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, f3g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    f3g_set_error("cudaGetSymbolAddress of the scratch array failed: %s", cudaGetErrorString(e));
     return 1;
   }
-  std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, f3g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      f3g_set_error("cudaGetSymbolAddress of the scratch array failed: %s", cudaGetErrorString(e));
-      return 1;
-    }
-    addr[dev] = (unsigned char *)p;
-  }
-  *out = addr[dev];
+  *out = (unsigned char *)p;
   return 0;
 }
 

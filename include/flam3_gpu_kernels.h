@@ -141,9 +141,8 @@ int flam3gpu_measure_atomic_rate(long long nbuckets, long long natomics, double 
  * 1.5 M FP32 or 0.75 M FP64 histogram buckets including the gutter); anything
  * larger returns 1 with an error naming the sizes.  Calls share the array:
  * each clears the histogram first, and calls that overlap on the GPU race.
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and keeps it; make that first call before any
- * stream capture, and do not call it on a device after cudaDeviceReset. */
+ * Each call looks up the array's address on the current device
+ * (cudaGetSymbolAddress). */
 int flam3gpu_render_noalloc(flam3_frame *f, void *out, int field, int nchan, int transp, stat_struct *stats);
 size_t flam3gpu_noalloc_capacity(void);
 
