@@ -15,8 +15,9 @@
  * and uploads each pass's header; this kernel fills in the rest.
  *
  * Work per sample: 256 palette entries (two HSV conversions per key), about
- * 230 blended doubles and two matrices per xform, up to 33 choice rows of
- * 16384 steps -- spread over the block's threads.
+ * 230 blended doubles and two matrices per xform, up to 33 choice rows --
+ * spread over the block's threads.  A choice row's 16384 dependent FP64 adds
+ * are replaced by the exact binade walk of f3g_choice.h.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -26,6 +27,7 @@
 #include "flam3_gpu.h"
 #include "f3g_common.h"
 #include "f3g_launch.h"
+#include "f3g_choice.h"
 
 #define PL_THREADS 256
 #define PL_VBLK 99 /* variation weights per xform */
@@ -381,31 +383,11 @@ __global__ void __launch_bounds__(PL_THREADS) k_plan(const unsigned char *__rest
     const int xi = r - 1;
     double dr = 0.0;
     for (int i = 0; i < nstd; i++) dr = xi >= 0 ? mac(dr, sdens[i], sch[xi * nstd + i]) : __dadd_rn(dr, sdens[i]);
-    int nb = 0, cur = 0, j = 0;
-    if (dr > 0.0) {
-      dr = dr / F3G_GRAIN;
-      double tt = xi >= 0 ? __dmul_rn(sdens[0], sch[xi * nstd]) : sdens[0];
-      double rr = 0.0;
-      for (int i = 0; i < F3G_GRAIN; i++) {
-        while (rr >= tt) {
-          j++;
-          if (j >= nx) {
-            err[blockIdx.x] = 2;
-            j = nx - 1;
-            break;
-          }
-          if (xi >= 0)
-            tt = mac(tt, sdens[j], j < nstd ? sch[xi * nstd + j] : 0.0);
-          else
-            tt = __dadd_rn(tt, sdens[j]);
-        }
-        while (cur < j && nb < F3G_MAX_XFORMS) {
-          p->brk[r][nb++] = (uint16_t)i;
-          cur++;
-        }
-        rr = __dadd_rn(rr, dr);
-      }
-    }
+    int nb = 0;
+    if (dr > 0.0 &&
+        f3g_choice_breakpoints(dr / F3G_GRAIN, sdens, xi >= 0 ? sch + xi * nstd : nullptr, nstd, nx, p->brk[r],
+                               F3G_MAX_XFORMS, &nb, nullptr))
+      err[blockIdx.x] = 2;
     p->nbrk[r] = (uint16_t)nb;
   }
 }

@@ -199,6 +199,14 @@ out:
   return rc;
 }
 
+int flam3gpu_choice_breakpoints(const double *d, const double *c, int nstd, int nx, int walk, uint16_t *brk,
+                                int *nbrk, int *moves) {
+  f3g_clear_error();
+  *nbrk = 0;
+  if (moves) *moves = 0;
+  return f3g_choice_breakpoints_host(d, c, nstd, nx, walk, brk, nbrk, moves);
+}
+
 int flam3gpu_xform_choice_table(flam3_genome *src, uint16_t *table, int *rows_out) {
   f3g_clear_error();
   f3g_ctx *c = f3g_get_ctx();

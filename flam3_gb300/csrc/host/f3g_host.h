@@ -82,6 +82,10 @@ int f3g_prepare_precalc_flags(flam3_genome *cp);
 void f3g_xform_precalc(flam3_genome *cp, int xi);
 /* builds the xform-choice table rows (flam3.c:76-224) and stores them as
  * breakpoints into pass; returns 0 on success */
+/* one choice row's breakpoints on the host: the reference's loop (walk 0) or
+ * the device planner's binade walk (walk 1) */
+int f3g_choice_breakpoints_host(const double *d, const double *c, int nstd, int nx, int walk, uint16_t *brk,
+                                int *nbrk, int *moves);
 int f3g_build_distrib(flam3_genome *cp, F3GPass *pass);
 /* fills the genome part of a pass from a prepared genome */
 int f3g_pack_genome(flam3_genome *cp, F3GPass *pass);

@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include "f3g_host.h"
+#include "../f3g_choice.h"
 
 void f3g_genome_free(flam3_genome *g) {
   if (g->xform) {
@@ -146,37 +147,43 @@ void f3g_xform_precalc(flam3_genome *cp, int xi) {
   xf->wedgeJulia_cn = xf->wedge_julia_dist / xf->wedge_julia_power / 2.0;
 }
 
-/* one table row (flam3.c:165-224): xi < 0 is the raw-weight row */
-static int chaos_row(flam3_genome *cp, int xi, unsigned short *row) {
-  int num_std = cp->num_xforms - (cp->final_xform_index >= 0);
-  double dr = 0.0;
-  for (int i = 0; i < num_std; i++) {
-    double d = cp->xform[i].density;
-    if (xi >= 0) d *= cp->chaos[xi][i];
-    if (d < 0.0) {
-      f3g_set_error("xform weight must be non-negative, not %g.", d);
+/* the step of a choice row (flam3.c:165-224): the sum of its weights
+ * d[i] (times the row's chaos entries c[i]; c NULL for the raw-weight row)
+ * over the standard xforms, divided by F3G_GRAIN */
+static int choice_step(const double *d, const double *c, int nstd, double *dr) {
+  double sum = 0.0;
+  for (int i = 0; i < nstd; i++) {
+    const double w = c ? d[i] * c[i] : d[i];
+    if (w < 0.0) {
+      f3g_set_error("xform weight must be non-negative, not %g.", w);
       return 1;
     }
-    dr += d;
+    sum += w;
   }
-  if (dr == 0.0) {
+  if (sum == 0.0) {
     f3g_set_error("cannot iterate empty flame.");
     return 1;
   }
-  dr = dr / F3G_GRAIN;
+  *dr = sum / F3G_GRAIN;
+  return 0;
+}
+
+/* one table row (flam3.c:165-224) over the weights d[0..nx) (a chaos row
+ * weights the standard xforms by c and the final xform by 0) */
+static int choice_row(const double *d, const double *c, int nstd, int nx, unsigned short *row) {
+  double dr;
+  if (choice_step(d, c, nstd, &dr)) return 1;
   int j = 0;
-  double t = cp->xform[0].density;
-  if (xi >= 0) t *= cp->chaos[xi][0];
+  double t = c ? d[0] * c[0] : d[0];
   double r = 0.0;
   for (int i = 0; i < F3G_GRAIN; i++) {
     while (r >= t) {
       j++;
-      if (j >= cp->num_xforms) { /* the reference would read past the xform array */
+      if (j >= nx) { /* the reference would read past the xform array */
         f3g_set_error("xform distribution overran the xform list");
         return 1;
       }
-      if (xi >= 0) t += cp->xform[j].density * (j < num_std ? cp->chaos[xi][j] : 0.0);
-      else t += cp->xform[j].density;
+      t += c ? d[j] * (j < nstd ? c[j] : 0.0) : d[j];
     }
     row[i] = (unsigned short)j;
     r += dr;
@@ -197,11 +204,48 @@ static int row_to_breakpoints(const unsigned short *row, uint16_t *brk, uint16_t
   return 0;
 }
 
+/* row xi of the genome's table (xi < 0: the raw-weight row) as breakpoints */
+static int chaos_row(flam3_genome *cp, int xi, unsigned short *row, uint16_t *brk, uint16_t *nbrk) {
+  const int nstd = cp->num_xforms - (cp->final_xform_index >= 0);
+  double d[F3G_MAX_XFORMS];
+  if (cp->num_xforms > F3G_MAX_XFORMS) {
+    f3g_set_error("genome has %d xforms; the library handles up to %d", cp->num_xforms, F3G_MAX_XFORMS);
+    return 1;
+  }
+  for (int i = 0; i < cp->num_xforms; i++) d[i] = cp->xform[i].density;
+  return choice_row(d, xi >= 0 ? cp->chaos[xi] : NULL, nstd, cp->num_xforms, row) ||
+         row_to_breakpoints(row, brk, nbrk);
+}
+
+int f3g_choice_breakpoints_host(const double *d, const double *c, int nstd, int nx, int walk, uint16_t *brk,
+                                int *nbrk, int *moves) {
+  if (nx < 1 || nx > F3G_MAX_XFORMS || nstd < 1 || nstd > nx) {
+    f3g_set_error("choice row of %d xforms (%d standard)", nx, nstd);
+    return 1;
+  }
+  if (!walk) {
+    unsigned short *row = (unsigned short *)malloc(F3G_GRAIN * sizeof(unsigned short));
+    uint16_t n = 0;
+    const int rc = !row || choice_row(d, c, nstd, nx, row) || row_to_breakpoints(row, brk, &n);
+    free(row);
+    *nbrk = n;
+    if (moves) *moves = F3G_GRAIN;
+    return rc;
+  }
+  double dr;
+  if (choice_step(d, c, nstd, &dr)) return 1;
+  if (f3g_choice_breakpoints(dr, d, c, nstd, nx, brk, F3G_MAX_XFORMS, nbrk, moves)) {
+    f3g_set_error("xform distribution overran the xform list");
+    return 1;
+  }
+  return 0;
+}
+
 int f3g_build_distrib(flam3_genome *cp, F3GPass *pass) {
   unsigned short *row = (unsigned short *)malloc(F3G_GRAIN * sizeof(unsigned short));
   int rc = 0;
   memset(pass->nbrk, 0, sizeof(pass->nbrk));
-  if (chaos_row(cp, -1, row) || row_to_breakpoints(row, pass->brk[0], &pass->nbrk[0])) {
+  if (chaos_row(cp, -1, row, pass->brk[0], &pass->nbrk[0])) {
     rc = 1;
     goto out;
   }
@@ -218,7 +262,7 @@ int f3g_build_distrib(flam3_genome *cp, F3GPass *pass) {
       for (int i = 0; i < cp->num_xforms; i++) {
         if (cp->final_xform_index == i) continue;
         dist_row++;
-        if (chaos_row(cp, i, row) || row_to_breakpoints(row, pass->brk[dist_row], &pass->nbrk[dist_row])) {
+        if (chaos_row(cp, i, row, pass->brk[dist_row], &pass->nbrk[dist_row])) {
           rc = 1;
           goto out;
         }

@@ -79,6 +79,8 @@ def load():
                                             C.POINTER(C.c_long), C.c_int]
     lib.flam3gpu_xform_choice_table.argtypes = [G, C.POINTER(C.c_uint16), C.POINTER(C.c_int)]
     lib.flam3gpu_plan_passes.argtypes = [F, C.c_int, C.c_void_p, C.c_int]
+    lib.flam3gpu_choice_breakpoints.argtypes = [dp, dp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint16),
+                                                C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.flam3gpu_pass_bytes.restype = C.c_size_t
     lib.flam3gpu_interpolate.argtypes = [G, C.c_int, C.c_double, C.c_double, G]
     lib.flam3gpu_estimate_bounding_box.argtypes = [G, C.c_double, C.c_int, dp, dp, C.POINTER(abi.randctx)]
@@ -240,6 +242,25 @@ def iterate_chains(genome, starts, n, fuse, seed, precision=64):
                                    C.byref(bad), precision):
         _err(lib, "iterate_chains")
     return out, bad.value
+
+
+def choice_breakpoints(weights, chaos=None, nstd=None, walk=False, moves=False):
+    """Breakpoints of one choice row on the host: weights of every xform
+    (the final one last), the row's chaos entries or None, built by the
+    reference's loop or (walk=True) the device planner's binade walk.
+    Returns the breakpoint list (and, with moves=True, the sequential steps
+    taken); raises Flam3GpuError on the reference's errors."""
+    lib = load()
+    d = np.ascontiguousarray(weights, dtype=np.float64)
+    nx = d.shape[0]
+    nstd = nx if nstd is None else nstd
+    c = None if chaos is None else np.ascontiguousarray(chaos, dtype=np.float64)
+    brk = (C.c_uint16 * 32)()
+    n, mv = C.c_int(0), C.c_int(0)
+    if lib.flam3gpu_choice_breakpoints(_dptr(d), None if c is None else _dptr(c), nstd, nx, 1 if walk else 0, brk,
+                                       C.byref(n), C.byref(mv)):
+        _err(lib, "choice_breakpoints")
+    return (list(brk)[:n.value], mv.value) if moves else list(brk)[:n.value]
 
 
 def xform_choice_table(genome):

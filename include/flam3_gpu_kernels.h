@@ -64,6 +64,17 @@ int flam3gpu_apply_xform(flam3_genome *cp, int fn, int n, const double *p_in,
  * entries and receives the row count in *rows. */
 int flam3gpu_xform_choice_table(flam3_genome *cp, uint16_t *table, int *rows);
 
+/* Host probe of one choice row (no GPU): the breakpoints of the row with
+ * xform weights d[0..nx) (times the row's chaos entries c[0..nstd), or c NULL
+ * for the raw-weight row), built by the reference's 16384-step loop
+ * (flam3.c:165-224; walk = 0) or by the binade walk the device planner uses
+ * (walk = 1).  brk gets up to 32 entries, *nbrk their count, *moves (if not
+ * NULL) the sequential steps taken (16384 for the loop; real steps plus
+ * closed-form runs for the walk); returns 1 with the reference's errors
+ * (negative or all-zero weights, a walk past the last xform). */
+int flam3gpu_choice_breakpoints(const double *d, const double *c, int nstd, int nx, int walk, uint16_t *brk,
+                                int *nbrk, int *moves);
+
 /* The passes (per temporal sample: interpolated genome, prepared xforms,
  * choice rows, colour map, camera) that flam3gpu_render would build for the
  * first batch of frame f, planned on the device (on_device = 1) or on host
