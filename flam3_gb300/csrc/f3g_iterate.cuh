@@ -467,6 +467,177 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
   bad_total += bad;
 }
 
+/* F3G_EXCHANGE: how mode 1 moves points between warps.
+ *   0: the block shuffle above -- every `shuffle_every` steps all warps
+ *      meet at a block barrier, so each round waits for the warp whose
+ *      xforms were the most expensive;
+ *   1 (default): a lagged exchange through two shared buffers and two
+ *      mbarriers -- a warp writes its points to the buffer of round h and
+ *      takes its next points from the buffer of round h-1, waiting only
+ *      until every warp has finished round h-1, so warps drift up to one
+ *      round apart instead of meeting every round. */
+#ifndef F3G_EXCHANGE
+#define F3G_EXCHANGE 1
+#endif
+
+/* shared-memory mbarrier helpers (PTX mbarrier.*; CTA scope) */
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+/* waits for the completion of the barrier's phase of parity `ph`; false when
+ * it has not completed within about two seconds (a lost arrival) */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned ph) {
+  const unsigned a = smem_addr(bar);
+  unsigned long long t0 = 0;
+  for (unsigned i = 0; i < (1u << 30); i++) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(a), "r"(ph)
+        : "memory");
+    if (ok) return true;
+    if ((i & 255) == 0) {
+      const unsigned long long t = global_ns();
+      if (i == 0) t0 = t;
+      else if (t - t0 > 2000000000ull) return false;
+    }
+  }
+  return false;
+}
+
+/* Block state of the lagged exchange: two mbarriers (one arrival per warp
+ * per round), the done-thread counts of the two buffers' rounds, the phase
+ * parities every thread tracks identically, an abort flag. */
+struct Exchange {
+  uint64_t bar[2];
+  int done[2];
+  int abort;
+};
+
+/* mode 1 with the lagged exchange (F3G_EXCHANGE 1).  The block keeps 2T
+ * points: T in registers, T in the buffer of the last round.  Round h: a
+ * thread runs `shuffle_every` steps on its point, waits for buffer (h-1)&1
+ * (every warp has written round h-1), takes the point at its slot there,
+ * writes its own point to buffer h&1 at the round's permuted slot and
+ * arrives.  A buffer is rewritten only after every thread waited for the
+ * other one, which each does after reading, so no read races a write.  A
+ * point is advanced every other round, so the thread discards 2 fuse +
+ * shuffle_every steps before plotting: every point then has at least `fuse`
+ * steps behind it.  Threads count themselves done (no samples left) into the
+ * round's count before arriving; when a round's count shows every thread
+ * done, all threads see it after the same wait and leave together.  `ph` holds the two
+ * barriers' phase parities (kept across chunks); false when a wait timed out. */
+template <typename R, bool FULL>
+__device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchange &xc, unsigned &ph,
+                                   long long local_chunk, int S, int shuffle_every, unsigned &bad_total,
+                                   unsigned &hits) {
+  const int T = blockDim.x, t = threadIdx.x, lane = t & 31, G = T >> 5, wl = t >> 5;
+  long long base = local_chunk * (long long)T * S;
+  long long n_chunk = s.samples - base;
+  if (n_chunk > (long long)T * S) n_chunk = (long long)T * S;
+  long long q = n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0);
+  /* buffer k: x, y, colour (R) and bad-value count (int) arrays of T each,
+   * at xb + k * half */
+  unsigned char *const xb = reinterpret_cast<unsigned char *>(buf);
+  const unsigned half = (unsigned)(sizeof(ShufPoint<R>) * T);
+  Rng rng;
+  rng.init(s.key0, s.key1, (uint32_t)local_chunk, (uint32_t)t, 0x5EEDu);
+  WarpWords ww;
+  ww.init(s.key0, s.key1, (uint32_t)local_chunk, (uint32_t)wl, (uint32_t)lane);
+  R px = u11<R>(rng.word()), py = u11<R>(rng.word()), pc = u01<R>(rng.word()), po = u01<R>(rng.word());
+  int consec = 0, lastxf = 0;
+  unsigned bad = 0;
+  const int rslot = t ^ ((t >> 5) & 31);
+  /* round -1: the second set of points, at the reading slots of round 0 */
+  {
+    const R ax = u11<R>(rng.word()), ay = u11<R>(rng.word()), ac = u01<R>(rng.word());
+    R *X = reinterpret_cast<R *>(xb + half);
+    X[rslot] = ax; X[T + rslot] = ay; X[2 * T + rslot] = ac;
+    reinterpret_cast<int *>(X + 3 * T)[rslot] = 0;
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&xc.bar[1]);
+  }
+  int fuse_left = 2 * s.fuse + shuffle_every;
+  long long remaining = q;
+  uint32_t rot = 0;
+  int seen0 = 0, seen1 = 0; /* the two buffers' done counts at their last read */
+  bool agg = F3G_AGG == 2 || (F3G_AGG == 1 && s.bucket_kind == F3G_BK_F64);
+  int probes = 0, dups = 0;
+  bool ok_all = true;
+  for (int round = 0;; round++) {
+    for (int k = 0; k < shuffle_every; k++) {
+      const uint32_t w = ww.word();
+      int fn = pick_xform(s, 0, w & (F3G_GRAIN - 1));
+      R qx, qy, qc, qo;
+      bool ok = chain_step<R, FULL, Rng>(s, fn, px, py, pc, po, consec, lastxf, bad, qx, qy, qc, qo, rng);
+      if (ok) {
+        if (fuse_left > 0) fuse_left--;
+        else if (remaining > 0) {
+          hits += plot(s, qx, qy, qc, qo, agg);
+          remaining--;
+        }
+      }
+    }
+    const int cur = round & 1, prev = cur ^ 1;
+    /* the points of round h-1 (the warp decides together, so a wait that
+     * ends at the time limit in one lane ends the exchange for all) */
+    if (!__all_sync(0xffffffffu, mbar_wait(&xc.bar[prev], (ph >> prev) & 1u))) {
+      xc.abort = 1;
+      ok_all = false;
+      break;
+    }
+    ph ^= 1u << prev;
+    const R *P = reinterpret_cast<const R *>(xb + prev * half);
+    const R nx_ = P[rslot], ny_ = P[T + rslot], nc_ = P[2 * T + rslot];
+    const int nq_ = reinterpret_cast<const int *>(P + 3 * T)[rslot];
+    const int d = xc.done[prev];
+    const int all_done = d - (prev ? seen1 : seen0) == T;
+    if (prev) seen1 = d;
+    else seen0 = d;
+    if (all_done) break; /* every thread had finished by round h-1 */
+    /* this round's points to buffer h&1: transpose lanes across warps, XOR
+     * the low five bits, rotate by whole 32-point segments (block-uniform
+     * amounts), at swizzled slots (32 distinct banks) */
+    rot += 0x9E3779B1u * (uint32_t)(round + 1);
+    const int x5 = (int)(rot >> 27), kr = (int)(rot >> 24) % G;
+    const int dst = (((lane * G + wl) ^ x5) + 32 * kr) & (T - 1);
+    const int wslot = dst ^ ((dst >> 5) & 31);
+    R *W = reinterpret_cast<R *>(xb + cur * half);
+    W[wslot] = px; W[T + wslot] = py; W[2 * T + wslot] = pc;
+    reinterpret_cast<int *>(W + 3 * T)[wslot] = consec;
+    const unsigned ndone = __popc(__ballot_sync(0xffffffffu, remaining == 0 && fuse_left == 0));
+    __syncwarp();
+    if (lane == 0) {
+      if (ndone) atomicAdd(&xc.done[cur], (int)ndone);
+      mbar_arrive(&xc.bar[cur]);
+    }
+    px = nx_; py = ny_; pc = nc_; consec = nq_;
+#if F3G_AGG == 1
+    if (!agg && probes < 4 && (round & 7) == 7) {
+      const int b = bucket_of(s, px, py);
+      const unsigned peers = __match_any_sync(0xffffffffu, b < 0 ? -1 - lane : b);
+      const unsigned shared = __ballot_sync(0xffffffffu, __popc(peers) > 1);
+      dups += __popc(shared) >= F3G_AGG_LANES;
+      if (++probes == 4) agg = dups >= 2;
+    }
+#endif
+  }
+  (void)po;
+  bad_total += bad;
+  return ok_all;
+}
+
 /* occupancy target: 4 blocks of 256 threads per SM for FP32 iteration (64
  * registers; measured 10 % faster than 3 blocks at 80 registers despite a
  * few spilled bytes), 2 for FP64 */
@@ -499,11 +670,23 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GI
   ShufPoint<R> *buf = reinterpret_cast<ShufPoint<R> *>(smem_raw + ((sizeof(PassS<R>) + 15) & ~(size_t)15));
   __shared__ long long sh_chunk;
   __shared__ int sh_item;
+#if F3G_EXCHANGE == 1
+  __shared__ Exchange xc;
+  unsigned ph = 0; /* phase parities of xc.bar[0..1] */
+  if (MODE == 1 && threadIdx.x == 0) {
+    mbar_init(&xc.bar[0], blockDim.x >> 5);
+    mbar_init(&xc.bar[1], blockDim.x >> 5);
+    xc.abort = 0;
+  }
+#endif
   int cur = -1;
   long long first = 0;
   unsigned bad = 0, hits = 0;
   for (;;) {
     if (threadIdx.x == 0) {
+#if F3G_EXCHANGE == 1
+      xc.done[0] = xc.done[1] = 0;
+#endif
       long long g = (long long)atomicAdd(&ctr->next_chunk, 1ull);
       int p = cur;
       if (g < total_chunks) {
@@ -533,15 +716,27 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GI
       __syncthreads();
     }
     long long local = g - chunk_prefix[p] + first;
+#if F3G_EXCHANGE == 1
+    if (MODE == 1) (void)run_chunk_warp_lag<R, FULL>(s, buf, xc, ph, local, s.S, shuffle_every, bad, hits);
+#else
     if (MODE == 1) run_chunk_warp<R, FULL>(s, buf, local, s.S, shuffle_every, bad, hits);
+#endif
     else run_chunk_thread<R, FULL>(s, local, s.S, bad, hits);
     __syncthreads();
+#if F3G_EXCHANGE == 1
+    if (MODE == 1 && xc.abort) {
+      /* an exchange wait timed out: report it and stop this block */
+      if (threadIdx.x == 0) atomicExch(&ctr->error, 1ull);
+      break;
+    }
+#endif
   }
   if (cur >= 0) flush_counts(s.counters, bad, hits);
 }
 
+/* pass + the exchange buffers of mode 1 (two rounds of points) */
 template <typename R> static size_t iterate_smem(int threads) {
-  return ((sizeof(PassS<R>) + 15) & ~(size_t)15) + sizeof(ShufPoint<R>) * (size_t)threads;
+  return ((sizeof(PassS<R>) + 15) & ~(size_t)15) + 2 * sizeof(ShufPoint<R>) * (size_t)threads;
 }
 
 template <typename R, bool FULL, int MODE>

@@ -278,6 +278,10 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
       goto done;
     }
     NCK(cudaMemcpy(&ctr, d_ctr, sizeof(ctr), cudaMemcpyDeviceToHost));
+    if (ctr.error) {
+      f3g_set_error("iterate kernel: a point-exchange wait timed out");
+      goto done;
+    }
     stats->badvals = (double)ctr.badvals;
     const double k1 = (cp.contrast * cp.brightness * 255.0 * 268.0) / 256;
     const double area = g.image_width * g.image_height / (ppux * ppuy);

@@ -937,6 +937,10 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         t_iter += ms;
         stats->badvals += (double)c->h_ctr->badvals;
         plotted += (double)c->h_ctr->plotted;
+        if (c->h_ctr->error) {
+          f3g_set_error("iterate kernel: a point-exchange wait timed out");
+          goto done;
+        }
         if (spec->progress) {
           double pct = 100.0 * ((double)batch + (double)hi / (double)total_chunks) / nbatches;
           int r = spec->progress(spec->progress_parameter, pct, 0, 0.0);
@@ -1157,6 +1161,10 @@ tail_fused:;
         t_iter += mi;
         stats->badvals += (double)c->h_ctr->badvals;
         plotted += (double)c->h_ctr->plotted;
+        if (c->h_ctr->error) {
+          f3g_set_error("iterate kernel: a point-exchange wait timed out");
+          goto done;
+        }
       }
       rv = 0;
       goto done;
@@ -1195,6 +1203,10 @@ tail_fused:;
       t_iter += mi;
       stats->badvals += (double)c->h_ctr->badvals;
       plotted += (double)c->h_ctr->plotted;
+      if (c->h_ctr->error) {
+        f3g_set_error("iterate kernel: a point-exchange wait timed out");
+        goto done;
+      }
     }
   }
   rv = 0;

@@ -104,7 +104,7 @@ typedef struct {
   F3GItem *h_items, *d_items;
   long long *h_prefix, *d_prefix;
   size_t cap; /* items */
-  F3GCounters *d_ctr; /* one per class */
+  F3GCounters *d_ctr, *h_ctr; /* one per class; pinned copy read when the round completes */
   cudaEvent_t ev, t0, t1; /* completion; timing of the round's launches */
   int in_use;
 } round_buf;
@@ -143,6 +143,7 @@ struct flam3gpu_service {
   round_buf rb[NRB];
   unsigned long long round_no;
   int paused; /* jobs the last round left out because their progress callback paused them */
+  char kernel_err[128]; /* set when an iterate launch reported an error: jobs finishing later fail */
   int inflight[NRB];
   tail_slot ts[NTAIL];
   unsigned long long tail_no;
@@ -598,7 +599,8 @@ flam3gpu_service *flam3gpu_service_create(const flam3gpu_service_config *cfg_in)
   for (int k = 0; ok && k < NRB; k++)
     ok = cudaEventCreateWithFlags(&s->rb[k].ev, cudaEventDisableTiming | cudaEventBlockingSync) == cudaSuccess &&
          cudaEventCreate(&s->rb[k].t0) == cudaSuccess && cudaEventCreate(&s->rb[k].t1) == cudaSuccess &&
-         cudaMalloc((void **)&s->rb[k].d_ctr, NCLASS * sizeof(F3GCounters)) == cudaSuccess;
+         cudaMalloc((void **)&s->rb[k].d_ctr, NCLASS * sizeof(F3GCounters)) == cudaSuccess &&
+         cudaMallocHost((void **)&s->rb[k].h_ctr, NCLASS * sizeof(F3GCounters)) == cudaSuccess;
   for (int k = 0; ok && k < NTAIL; k++)
     ok = cudaEventCreateWithFlags(&s->ts[k].ev, cudaEventBlockingSync) == cudaSuccess &&
          cudaEventCreate(&s->ts[k].t0) == cudaSuccess;
@@ -1074,12 +1076,18 @@ static void complete_job(flam3gpu_service *s, f3g_job *j) {
   pthread_mutex_unlock(&s->mu);
 }
 
+static int rounds_in_flight(flam3gpu_service *s);
+
 static void finish_slot(flam3gpu_service *s, tail_slot *t) {
   float ms = 0;
   if (cudaEventElapsedTime(&ms, t->t0, t->ev) == cudaSuccess) s->g_tail += ms * 1e-3;
+  (void)rounds_in_flight(s); /* the rounds before this tail are done: read their error flags */
   for (int i = 0; i < t->njobs; i++) {
     f3g_job *j = t->jobs[i];
-    if (j->batch == j->nbatches - 1) complete_job(s, j);
+    if (s->kernel_err[0]) {
+      remove_active(s, j);
+      fail_job(s, j, s->kernel_err);
+    } else if (j->batch == j->nbatches - 1) complete_job(s, j);
     else {
       j->batch++;
       j->cursor = 0;
@@ -1311,6 +1319,9 @@ static int issue_round(flam3gpu_service *s) {
     if (e) err = 1;
   }
   cudaEventRecord(r->t1, st);
+  if (!err && cudaMemcpyAsync(r->h_ctr, r->d_ctr, NCLASS * sizeof(F3GCounters), cudaMemcpyDeviceToHost, st) !=
+                  cudaSuccess)
+    err = 1;
   cudaEventRecord(r->ev, st);
   cudaEventRecord(s->ev_last[si], st);
   r->in_use = 1;
@@ -1335,6 +1346,9 @@ static int issue_round(flam3gpu_service *s) {
 static void round_done(flam3gpu_service *s, round_buf *r) {
   float ms = 0;
   if (cudaEventElapsedTime(&ms, r->t0, r->t1) == cudaSuccess) s->g_iter += ms * 1e-3;
+  for (int c = 0; c < NCLASS; c++)
+    if (r->h_ctr[c].error && !s->kernel_err[0])
+      snprintf(s->kernel_err, sizeof(s->kernel_err), "iterate kernel: a point-exchange wait timed out");
   r->in_use = 0;
 }
 
@@ -1604,6 +1618,7 @@ void flam3gpu_service_destroy(flam3gpu_service *s) {
     if (s->rb[k].d_items) cudaFree(s->rb[k].d_items);
     if (s->rb[k].d_prefix) cudaFree(s->rb[k].d_prefix);
     if (s->rb[k].d_ctr) cudaFree(s->rb[k].d_ctr);
+    if (s->rb[k].h_ctr) cudaFreeHost(s->rb[k].h_ctr);
     if (s->rb[k].ev) cudaEventDestroy(s->rb[k].ev);
     if (s->rb[k].t0) cudaEventDestroy(s->rb[k].t0);
     if (s->rb[k].t1) cudaEventDestroy(s->rb[k].t1);
