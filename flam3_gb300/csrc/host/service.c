@@ -72,6 +72,7 @@ typedef struct f3g_job {
   int nbatches, ntemporal, threads, precision;
   int fused_de, fused_log, need_acc, count_any, tile, band_de;
   int aborted; /* the progress callback asked to abort: no more rounds, no tail, output untouched */
+  double sort_key; /* the round's ordering key (cfg.order 1 and 2) */
   F3GPass *h_passes;      /* nbatches * ntemporal */
   long long *pass_prefix; /* per batch: ntemporal+1 chunk offsets, concatenated */
   batch_plan *bp;
@@ -153,6 +154,7 @@ struct flam3gpu_service {
   double c_done, c_failed, c_rounds, c_launches, c_graphs, c_inst, c_plotted, c_h2d, c_d2h;
   double h_admit, h_round, h_tail, h_done, h_wait; /* service-thread seconds by activity */
   double g_iter, g_tail;                           /* device seconds of iterate rounds and of tails */
+  double c_samples;                                /* samples issued in iterate rounds */
   double t_first_admit, t_last_done;
 };
 
@@ -564,6 +566,35 @@ static int job_remaining_cmp(const void *a, const void *b) {
   return x->ticket < y->ticket ? -1 : (x->ticket > y->ticket);
 }
 
+/* higher sort key first, then arrival order */
+static int job_key_cmp(const void *a, const void *b) {
+  const f3g_job *x = *(f3g_job *const *)a, *y = *(f3g_job *const *)b;
+  if (x->sort_key > y->sort_key) return -1;
+  if (x->sort_key < y->sort_key) return 1;
+  return x->ticket < y->ticket ? -1 : (x->ticket > y->ticket);
+}
+
+/* orders a round's candidate jobs by the service's policy (cfg.order) */
+static void order_jobs(flam3gpu_service *s, f3g_job **cand, int nc) {
+  if (s->cfg.order == 1) {
+    /* response ratio: remaining time from the service's measured sample
+     * rate (samples per second of iterate GPU time) */
+    const double rate = s->g_iter > 0.05 && s->c_samples > 0 ? s->c_samples / s->g_iter : 4.0e10;
+    const double now = now_s();
+    for (int i = 0; i < nc; i++) {
+      f3g_job *j = cand[i];
+      double rem = (j->total_samples - j->done_samples) / rate;
+      if (rem < 1e-4) rem = 1e-4;
+      j->sort_key = (now - j->t_submit + rem) / rem;
+    }
+    qsort(cand, (size_t)nc, sizeof(f3g_job *), job_key_cmp);
+  } else if (s->cfg.order == 2) {
+    for (int i = 0; i < nc; i++) cand[i]->sort_key = -(double)cand[i]->ticket;
+    qsort(cand, (size_t)nc, sizeof(f3g_job *), job_key_cmp);
+  } else
+    qsort(cand, (size_t)nc, sizeof(f3g_job *), job_remaining_cmp);
+}
+
 flam3gpu_service *flam3gpu_service_create(const flam3gpu_service_config *cfg_in) {
   f3g_clear_error();
   flam3gpu_service *s = (flam3gpu_service *)calloc(1, sizeof(*s));
@@ -579,6 +610,7 @@ flam3gpu_service *flam3gpu_service_create(const flam3gpu_service_config *cfg_in)
   if (s->cfg.max_inflight > NRB - 1) s->cfg.max_inflight = NRB - 1;
   if (s->cfg.tail_branches < 1) s->cfg.tail_branches = 1;
   if (s->cfg.tail_branches > NBRANCH) s->cfg.tail_branches = NBRANCH;
+  if (s->cfg.order < 0 || s->cfg.order > 2) s->cfg.order = 0;
   if (cudaGetDevice(&s->device) != cudaSuccess ||
       cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device) != cudaSuccess) {
     f3g_set_error("no CUDA device available");
@@ -1187,8 +1219,8 @@ static int issue_round(flam3gpu_service *s) {
     free(takes);
     return ntails > 0;
   }
-  qsort(cand, (size_t)nc, sizeof(f3g_job *), job_remaining_cmp);
-  /* shortest remaining job first, up to the round's sample budget; the
+  order_jobs(s, cand, nc);
+  /* jobs in the policy's order (shortest remaining first by default), up to the round's sample budget; the
    * automatic budget gives every resident block at least 4 chunks of the
    * coarsest job, so the round's last wave wastes little */
   double budget;
@@ -1254,6 +1286,7 @@ static int issue_round(flam3gpu_service *s) {
     if (!ti) break;
     j->pass_hint = p < j->ntemporal ? p : j->ntemporal - 1;
     j->done_samples += (double)takes[i] * j->threads * b->S;
+    s->c_samples += (double)takes[i] * j->threads * b->S;
     j->cursor = end;
     j->rounds++;
     if (j->t_first == 0) j->t_first = now_s();

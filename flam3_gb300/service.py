@@ -17,7 +17,8 @@ from . import abi, render
 class ServiceConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("round_samples", C.c_longlong), ("max_active", C.c_int),
                 ("tail_graphs", C.c_int), ("streams", C.c_int), ("use_tuning", C.c_int),
-                ("max_inflight", C.c_int), ("tail_branches", C.c_int), ("reserved", C.c_int * 6)]
+                ("max_inflight", C.c_int), ("tail_branches", C.c_int), ("order", C.c_int),
+                ("reserved", C.c_int * 5)]
 
 
 _BOUND = False

@@ -54,7 +54,11 @@ typedef struct {
   int use_tuning;           /* 1: apply the autotuned table (flam3gpu_autotune) to new jobs */
   int max_inflight;         /* iterate rounds queued on the device at once (default 2) */
   int tail_branches;        /* parallel branches of a round's tail graph with tail_graphs 2 (default 1) */
-  int reserved[6];
+  int order;                /* which admitted jobs a round serves first: 0 (default) the shortest
+                               remaining work; 1 the highest response ratio, (waiting time + remaining
+                               time) / remaining time, so long jobs gain priority as they wait; 2 arrival
+                               order */
+  int reserved[5];
 } flam3gpu_service_config;
 
 void flam3gpu_service_default_config(flam3gpu_service_config *cfg);
