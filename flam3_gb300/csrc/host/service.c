@@ -554,6 +554,7 @@ void flam3gpu_service_default_config(flam3gpu_service_config *cfg) {
   cfg->use_tuning = 1;
   cfg->max_inflight = 2;
   cfg->tail_branches = 1;
+  cfg->order = 1;
 }
 
 static void *service_main(void *arg);

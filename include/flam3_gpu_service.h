@@ -54,10 +54,10 @@ typedef struct {
   int use_tuning;           /* 1: apply the autotuned table (flam3gpu_autotune) to new jobs */
   int max_inflight;         /* iterate rounds queued on the device at once (default 2) */
   int tail_branches;        /* parallel branches of a round's tail graph with tail_graphs 2 (default 1) */
-  int order;                /* which admitted jobs a round serves first: 0 (default) the shortest
-                               remaining work; 1 the highest response ratio, (waiting time + remaining
-                               time) / remaining time, so long jobs gain priority as they wait; 2 arrival
-                               order */
+  int order;                /* which admitted jobs a round serves first: 1 (default) the highest
+                               response ratio, (waiting time + remaining time) / remaining time, so short
+                               jobs pass long ones and long jobs gain priority as they wait; 0 the
+                               shortest remaining work; 2 arrival order */
   int reserved[5];
 } flam3gpu_service_config;
 

@@ -259,3 +259,40 @@ def test_progress_callback_abort_pause_and_batch(gpulib):
     Fb.f.progress = batch_cb
     (out_b, _), = service.render_batch([Fb])
     assert len(calls["batch"]) >= 1 and out_b.mean() > 1.0
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+def test_round_order_policies(gpulib, order):
+    """A long job submitted just before short ones: shortest-remaining (0)
+    and response-ratio (1) ordering let the short jobs pass it, arrival
+    order (2) finishes it first; every image still equals the plain render."""
+    import time
+
+    def mk(size, q, seed):
+        G = gm.small_genome(seed)
+        gm.resize(G, size, size)
+        G.g.sample_density = q
+        return gm.Frame(G, bits=33, seed="order-%d-%d" % (order, seed))
+
+    frames = [mk(512, 300.0, 0)] + [mk(64, 20.0, k) for k in range(1, 5)]
+    done = []
+    with service.Service(order=order, round_samples=1 << 22) as svc:
+        # both arms warm (allocations, graphs) before the timed submissions
+        svc.wait(svc.submit(mk(64, 5.0, 9)))
+        subs = []
+        for F in frames:
+            t0 = time.perf_counter()
+            subs.append((t0, svc.submit(F)))
+        for t0, tk in subs:
+            img, st, times = svc.wait(tk)
+            done.append((t0 + times[2] * 1e-3, img))
+    big = done[0][0]
+    small = [d for d, _ in done[1:]]
+    if order == 2:
+        assert big < min(small), (big, small)
+    else:
+        assert max(small) < big, (big, small)
+    for (_, img), F in zip(done, [mk(512, 300.0, 0)] + [mk(64, 20.0, k) for k in range(1, 5)]):
+        ref, _ = render.render(F)
+        ok, info = close_images(img, ref)
+        assert ok, info
