@@ -285,6 +285,62 @@ __device__ __forceinline__ bool chain_step(const PassS<R> &s, int fn, R &px, R &
   return true;
 }
 
+/* F3G_LEAN_RNG: 1 -- the iterate kernels' random streams read the pass key
+ * and chunk index from shared memory at each refill (ChunkRng,
+ * ChunkWarpWords: 24 fewer spilled bytes in mode 1); 0 (default) -- they
+ * hold them in registers (Rng, WarpWords), measured 1 % faster on the
+ * 1920x1080 still (48.4 against 47.9 Giter/s).  The words are the same
+ * either way. */
+#ifndef F3G_LEAN_RNG
+#define F3G_LEAN_RNG 0
+#endif
+
+/* The random streams of the chunk a block is running: the pass key and the
+ * chunk's counter word, set by thread 0 before the chunk starts.  The
+ * streams below read them at each refill instead of holding them in
+ * registers (the iterate kernel runs at its 64-register cap). */
+static __shared__ uint32_t f3g_chunk_ctx[3]; /* key0, key1, chunk */
+
+/* Per-thread word stream of a chunk: Philox blocks of counter (chunk, k,
+ * thread, 0x5EED) under the pass key, k = 0, 1, ...; four words per block
+ * in order.  Registers: the block's four words and the word count. */
+struct ChunkRng {
+  uint32_t b0, b1, b2, b3, m;
+  __device__ __forceinline__ void init() { m = 0; }
+  __device__ __forceinline__ uint32_t word() {
+    if ((m & 3u) == 0) {
+      const uint4 r = philox_block(f3g_chunk_ctx[2], m >> 2, threadIdx.x, 0x5EEDu, f3g_chunk_ctx[0], f3g_chunk_ctx[1]);
+      b0 = r.x; b1 = r.y; b2 = r.z; b3 = r.w;
+    }
+    const uint32_t c = m & 3u;
+    m++;
+    return c == 0 ? b0 : c == 1 ? b1 : c == 2 ? b2 : b3;
+  }
+};
+
+/* Warp-shared stream of xform-choice words: lane L holds words 4L..4L+3 of
+ * the current 128-word block, counter (chunk, k, 0xC0DE0000 | warp, L) under
+ * the pass key, so one Philox call per lane serves 128 steps of the warp;
+ * word n is read from lane (n / 4) % 32 with one shuffle.  The counters are
+ * disjoint from the per-thread streams (third word = thread index <
+ * 0xC0DE0000).  Warp-uniform: every lane calls word() at the same step. */
+struct ChunkWarpWords {
+  uint32_t b0, b1, b2, b3, n;
+  __device__ __forceinline__ void init() { n = 0; }
+  __device__ __forceinline__ uint32_t word() {
+    if ((n & 127u) == 0) {
+      const uint4 r = philox_block(f3g_chunk_ctx[2], n >> 7, 0xC0DE0000u | (threadIdx.x >> 5), threadIdx.x & 31u,
+                                   f3g_chunk_ctx[0], f3g_chunk_ctx[1]);
+      b0 = r.x; b1 = r.y; b2 = r.z; b3 = r.w;
+    }
+    const uint32_t c = n & 3u;
+    const uint32_t mine = c == 0 ? b0 : c == 1 ? b1 : c == 2 ? b2 : b3;
+    const uint32_t w = __shfl_sync(0xffffffffu, mine, (n >> 2) & 31u);
+    n++;
+    return w;
+  }
+};
+
 /* mode 0: independent chains, one per thread */
 template <typename R, bool FULL>
 __device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, int S, unsigned &bad_total,
@@ -293,18 +349,25 @@ __device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, int S
   long long base = local_chunk * (long long)T * S;
   long long n_chunk = s.samples - base;
   if (n_chunk > (long long)T * S) n_chunk = (long long)T * S;
-  long long q = n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0);
+  const int q = (int)(n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0));
+#if F3G_LEAN_RNG
+  ChunkRng rng;
+  rng.init();
+  typedef ChunkRng RngT;
+#else
   Rng rng;
   rng.init(s.key0, s.key1, (uint32_t)local_chunk, (uint32_t)t, 0x5EEDu);
+  typedef Rng RngT;
+#endif
   R px = u11<R>(rng.word()), py = u11<R>(rng.word()), pc = u01<R>(rng.word()), po = u01<R>(rng.word());
   int consec = 0, lastxf = 0;
   unsigned bad = 0;
   const int total = s.fuse;
-  for (long long i = -total; i < q;) {
+  for (int i = -total; i < q;) {
     int row = s.chaos_enable ? min(lastxf, s.num_std) : 0;
     int fn = pick_xform(s, row, rng.word() & (F3G_GRAIN - 1));
     R qx, qy, qc, qo;
-    if (!chain_step<R, FULL, Rng>(s, fn, px, py, pc, po, consec, lastxf, bad, qx, qy, qc, qo, rng)) continue;
+    if (!chain_step<R, FULL, RngT>(s, fn, px, py, pc, po, consec, lastxf, bad, qx, qy, qc, qo, rng)) continue;
     if (i >= 0) hits += plot(s, qx, qy, qc, qo);
     i++;
   }
@@ -517,11 +580,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned ph) {
 }
 
 /* Block state of the lagged exchange: two mbarriers (one arrival per warp
- * per round), the done-thread counts of the two buffers' rounds, the phase
- * parities every thread tracks identically, an abort flag. */
+ * per round), the done-thread counts of rounds h mod 4, an abort flag. */
 struct Exchange {
   uint64_t bar[2];
-  int done[2];
+  int done[4];
   int abort;
 };
 
@@ -534,27 +596,40 @@ struct Exchange {
  * other one, which each does after reading, so no read races a write.  A
  * point is advanced every other round, so the thread discards 2 fuse +
  * shuffle_every steps before plotting: every point then has at least `fuse`
- * steps behind it.  Threads count themselves done (no samples left) into the
- * round's count before arriving; when a round's count shows every thread
- * done, all threads see it after the same wait and leave together.  `ph` holds the two
- * barriers' phase parities (kept across chunks); false when a wait timed out. */
+ * steps behind it.  Threads add themselves to the round's done count (no
+ * samples left) before arriving; when the count of round h-1 is the whole
+ * block, every thread sees it after the same wait and all leave together.
+ * The count of round h+2 is cleared in round h, after every thread has read
+ * it (in round h-1) and before anyone adds to it (in round h+2).  `ph` holds
+ * the two barriers' phase parities (kept across chunks); false when a wait
+ * timed out. */
 template <typename R, bool FULL>
 __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchange &xc, unsigned &ph,
                                    long long local_chunk, int S, int shuffle_every, unsigned &bad_total,
                                    unsigned &hits) {
   const int T = blockDim.x, t = threadIdx.x, lane = t & 31, G = T >> 5, wl = t >> 5;
-  long long base = local_chunk * (long long)T * S;
+  const long long base = local_chunk * (long long)T * S;
   long long n_chunk = s.samples - base;
   if (n_chunk > (long long)T * S) n_chunk = (long long)T * S;
-  long long q = n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0);
+  /* samples of this thread (at most S) */
+  int remaining = (int)(n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0));
   /* buffer k: x, y, colour (R) and bad-value count (int) arrays of T each,
    * at xb + k * half */
   unsigned char *const xb = reinterpret_cast<unsigned char *>(buf);
   const unsigned half = (unsigned)(sizeof(ShufPoint<R>) * T);
+#if F3G_LEAN_RNG
+  ChunkRng rng;
+  rng.init();
+  ChunkWarpWords ww;
+  ww.init();
+  typedef ChunkRng RngT;
+#else
   Rng rng;
   rng.init(s.key0, s.key1, (uint32_t)local_chunk, (uint32_t)t, 0x5EEDu);
   WarpWords ww;
   ww.init(s.key0, s.key1, (uint32_t)local_chunk, (uint32_t)wl, (uint32_t)lane);
+  typedef Rng RngT;
+#endif
   R px = u11<R>(rng.word()), py = u11<R>(rng.word()), pc = u01<R>(rng.word()), po = u01<R>(rng.word());
   int consec = 0, lastxf = 0;
   unsigned bad = 0;
@@ -569,18 +644,18 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     if (lane == 0) mbar_arrive(&xc.bar[1]);
   }
   int fuse_left = 2 * s.fuse + shuffle_every;
-  long long remaining = q;
   uint32_t rot = 0;
-  int seen0 = 0, seen1 = 0; /* the two buffers' done counts at their last read */
-  bool agg = F3G_AGG == 2 || (F3G_AGG == 1 && s.bucket_kind == F3G_BK_F64);
-  int probes = 0, dups = 0;
+  /* bucket-sharing probes: bits 0-2 probes taken, 3-5 probes with shared
+   * buckets, bit 6 aggregation on */
+  int agg_state = (F3G_AGG == 2 || (F3G_AGG == 1 && s.bucket_kind == F3G_BK_F64)) ? 64 : 0;
   bool ok_all = true;
   for (int round = 0;; round++) {
+    const bool agg = agg_state & 64;
     for (int k = 0; k < shuffle_every; k++) {
       const uint32_t w = ww.word();
       int fn = pick_xform(s, 0, w & (F3G_GRAIN - 1));
       R qx, qy, qc, qo;
-      bool ok = chain_step<R, FULL, Rng>(s, fn, px, py, pc, po, consec, lastxf, bad, qx, qy, qc, qo, rng);
+      bool ok = chain_step<R, FULL, RngT>(s, fn, px, py, pc, po, consec, lastxf, bad, qx, qy, qc, qo, rng);
       if (ok) {
         if (fuse_left > 0) fuse_left--;
         else if (remaining > 0) {
@@ -601,11 +676,8 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     const R *P = reinterpret_cast<const R *>(xb + prev * half);
     const R nx_ = P[rslot], ny_ = P[T + rslot], nc_ = P[2 * T + rslot];
     const int nq_ = reinterpret_cast<const int *>(P + 3 * T)[rslot];
-    const int d = xc.done[prev];
-    const int all_done = d - (prev ? seen1 : seen0) == T;
-    if (prev) seen1 = d;
-    else seen0 = d;
-    if (all_done) break; /* every thread had finished by round h-1 */
+    if (xc.done[(round - 1) & 3] == T) break; /* every thread had finished by round h-1 */
+    if (t == 0) xc.done[(round + 2) & 3] = 0;
     /* this round's points to buffer h&1: transpose lanes across warps, XOR
      * the low five bits, rotate by whole 32-point segments (block-uniform
      * amounts), at swizzled slots (32 distinct banks) */
@@ -619,17 +691,17 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     const unsigned ndone = __popc(__ballot_sync(0xffffffffu, remaining == 0 && fuse_left == 0));
     __syncwarp();
     if (lane == 0) {
-      if (ndone) atomicAdd(&xc.done[cur], (int)ndone);
+      if (ndone) atomicAdd(&xc.done[round & 3], (int)ndone);
       mbar_arrive(&xc.bar[cur]);
     }
     px = nx_; py = ny_; pc = nc_; consec = nq_;
 #if F3G_AGG == 1
-    if (!agg && probes < 4 && (round & 7) == 7) {
+    if (!(agg_state & 64) && (agg_state & 7) < 4 && (round & 7) == 7) {
       const int b = bucket_of(s, px, py);
       const unsigned peers = __match_any_sync(0xffffffffu, b < 0 ? -1 - lane : b);
       const unsigned shared = __ballot_sync(0xffffffffu, __popc(peers) > 1);
-      dups += __popc(shared) >= F3G_AGG_LANES;
-      if (++probes == 4) agg = dups >= 2;
+      agg_state += 1 + (__popc(shared) >= F3G_AGG_LANES ? 8 : 0);
+      if ((agg_state & 7) == 4 && ((agg_state >> 3) & 7) >= 2) agg_state |= 64;
     }
 #endif
   }
@@ -685,7 +757,7 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GI
   for (;;) {
     if (threadIdx.x == 0) {
 #if F3G_EXCHANGE == 1
-      xc.done[0] = xc.done[1] = 0;
+      xc.done[0] = xc.done[1] = xc.done[2] = xc.done[3] = 0;
 #endif
       long long g = (long long)atomicAdd(&ctr->next_chunk, 1ull);
       int p = cur;
@@ -699,6 +771,11 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GI
           }
           p = lo;
         }
+        /* the chunk's random streams: pass key, chunk index within the pass */
+        const F3GPass *ps = items[p].pass;
+        f3g_chunk_ctx[0] = ps->key[0];
+        f3g_chunk_ctx[1] = ps->key[1];
+        f3g_chunk_ctx[2] = (uint32_t)(g - chunk_prefix[p] + items[p].chunk_first);
       }
       sh_chunk = g;
       sh_item = p;
