@@ -119,7 +119,9 @@ typedef struct {
   void *buckets;
   void *count;              /* optional count plane, NULL if A == count */
   int bucket_kind;
-  int S;                    /* samples per thread per chunk: a chunk is blockDim*S samples */
+  int S;                    /* samples per thread per chunk: a chunk is blockDim*S samples, */
+  int S_tail;               /* except chunks chunk_tail.. of the pass, which hold blockDim*S_tail */
+  int64_t chunk_tail;       /* (0 < S_tail <= S; S_tail 0: every chunk holds blockDim*S) */
   unsigned long long *counters; /* [0] bad values, [1] samples plotted (device) */
   /* --- xforms last: a pass is uploaded up to its last used xform ------ */
   F3GXform xf[F3G_MAX_XFORMS];

@@ -41,8 +41,8 @@ namespace f3g {
 
 template <typename R> struct PassS {
   int num_xforms, num_std, final_index, final_enable, chaos_enable, fuse, mode, full;
-  int width, height, nbuckets, rotate, cmap_size, palette_mode, bucket_kind, S, trunc;
-  long long samples, nchunks;
+  int width, height, nbuckets, rotate, cmap_size, palette_mode, bucket_kind, S, S_tail, trunc;
+  long long samples, nchunks, chunk_tail;
   unsigned long long *counters;
   uint32_t key0, key1;
   R b0, b1, b2, b3, r00, r01, r10, r11, rcx, rcy, ws0, wb0s0, hs1, hb1s1;
@@ -81,6 +81,8 @@ __device__ void stage_pass(PassS<R> &s, const F3GPass *__restrict__ p) {
     s.dws0 = p->ws0; s.dwb0s0 = p->wb0s0; s.dhs1 = p->hs1; s.dhb1s1 = p->hb1s1;
     s.buckets = p->buckets; s.count = p->count;
     s.S = p->S; s.counters = p->counters;
+    s.S_tail = p->S_tail > 0 ? p->S_tail : p->S;
+    s.chunk_tail = p->S_tail > 0 ? p->chunk_tail : p->nchunks;
   }
   const int nx = p->num_xforms;
   const int rows = p->num_std + 1;
@@ -343,12 +345,11 @@ struct ChunkWarpWords {
 
 /* mode 0: independent chains, one per thread */
 template <typename R, bool FULL>
-__device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, int S, unsigned &bad_total,
-                                 unsigned &hits) {
+__device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, long long base, long long len,
+                                 unsigned &bad_total, unsigned &hits) {
   const int T = blockDim.x, t = threadIdx.x;
-  long long base = local_chunk * (long long)T * S;
   long long n_chunk = s.samples - base;
-  if (n_chunk > (long long)T * S) n_chunk = (long long)T * S;
+  if (n_chunk > len) n_chunk = len;
   const int q = (int)(n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0));
 #if F3G_LEAN_RNG
   ChunkRng rng;
@@ -441,12 +442,11 @@ struct WarpWords {
 
 /* mode 1: warp-coherent xform choice plus block-wide point shuffles */
 template <typename R, bool FULL>
-__device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long local_chunk, int S, int shuffle_every,
-                               unsigned &bad_total, unsigned &hits) {
+__device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long local_chunk, long long base,
+                               long long len, int shuffle_every, unsigned &bad_total, unsigned &hits) {
   const int T = blockDim.x, t = threadIdx.x, lane = t & 31, nwarps = T >> 5;
-  long long base = local_chunk * (long long)T * S;
   long long n_chunk = s.samples - base;
-  if (n_chunk > (long long)T * S) n_chunk = (long long)T * S;
+  if (n_chunk > len) n_chunk = len;
   long long q = n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0);
   R *bx = reinterpret_cast<R *>(buf), *by = bx + T, *bc = by + T;
   int *bq = reinterpret_cast<int *>(bc + T);
@@ -605,12 +605,11 @@ struct Exchange {
  * timed out. */
 template <typename R, bool FULL>
 __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchange &xc, unsigned &ph,
-                                   long long local_chunk, int S, int shuffle_every, unsigned &bad_total,
-                                   unsigned &hits) {
+                                   long long local_chunk, long long base, long long len, int shuffle_every,
+                                   unsigned &bad_total, unsigned &hits) {
   const int T = blockDim.x, t = threadIdx.x, lane = t & 31, G = T >> 5, wl = t >> 5;
-  const long long base = local_chunk * (long long)T * S;
   long long n_chunk = s.samples - base;
-  if (n_chunk > (long long)T * S) n_chunk = (long long)T * S;
+  if (n_chunk > len) n_chunk = len;
   /* samples of this thread (at most S) */
   int remaining = (int)(n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0));
   /* buffer k: x, y, colour (R) and bad-value count (int) arrays of T each,
@@ -793,12 +792,22 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GI
       __syncthreads();
     }
     long long local = g - chunk_prefix[p] + first;
+    /* the chunk's samples: blockDim*S each up to chunk_tail, blockDim*S_tail after */
+    const long long TT = blockDim.x;
+    long long base, len;
+    if (local < s.chunk_tail) {
+      base = local * TT * s.S;
+      len = TT * s.S;
+    } else {
+      base = s.chunk_tail * TT * s.S + (local - s.chunk_tail) * TT * s.S_tail;
+      len = TT * s.S_tail;
+    }
 #if F3G_EXCHANGE == 1
-    if (MODE == 1) (void)run_chunk_warp_lag<R, FULL>(s, buf, xc, ph, local, s.S, shuffle_every, bad, hits);
+    if (MODE == 1) (void)run_chunk_warp_lag<R, FULL>(s, buf, xc, ph, local, base, len, shuffle_every, bad, hits);
 #else
-    if (MODE == 1) run_chunk_warp<R, FULL>(s, buf, local, s.S, shuffle_every, bad, hits);
+    if (MODE == 1) run_chunk_warp<R, FULL>(s, buf, local, base, len, shuffle_every, bad, hits);
 #endif
-    else run_chunk_thread<R, FULL>(s, local, s.S, bad, hits);
+    else run_chunk_thread<R, FULL>(s, local, base, len, bad, hits);
     __syncthreads();
 #if F3G_EXCHANGE == 1
     if (MODE == 1 && xc.abort) {

@@ -240,19 +240,13 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
     if (occ < 1) occ = 1;
     const int blocks = f3g_opts.blocks > 0 ? f3g_opts.blocks : nsm * occ;
     const int S = f3g_chunk_samples(nullptr, batch_samples, threads, blocks, spec->sub_batch_size);
-    long long total_chunks = 0;
+    const long long total_chunks = f3g_chunk_passes(passes, ntemporal, threads, blocks, S, prefix);
     for (int ts = 0; ts < ntemporal; ts++) {
       passes[ts].count = use_count ? d_count : nullptr;
-      passes[ts].S = S;
       passes[ts].counters = &d_ctr->badvals;
       items[ts].pass = d_passes + ts;
       items[ts].chunk_first = 0;
-      passes[ts].chunk_begin = total_chunks;
-      passes[ts].nchunks = (passes[ts].samples + (long long)threads * S - 1) / ((long long)threads * S);
-      prefix[ts] = total_chunks;
-      total_chunks += passes[ts].nchunks;
     }
-    prefix[ntemporal] = total_chunks;
     for (size_t i = 0; i < F3G_FILTER_FLOATS(g.filter_width); i++) fbuf[i] = (float)filter[i];
     if (de_on) {
       f3g_de_kernel_info(mfi, ks, de_w, de_c, fbuf + F3G_FILTER_FLOATS(g.filter_width));

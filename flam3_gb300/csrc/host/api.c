@@ -52,7 +52,8 @@ int flam3gpu_set_options(const flam3gpu_options *o) {
     f3g_set_error("threads_per_block must be a power of two in [32, 256]");
     return 1;
   }
-  if (o->shuffle_every < 0 || o->blocks < 0 || o->chain_samples < 0) {
+  if (o->shuffle_every < 0 || o->blocks < 0 || o->chain_samples < 0 || o->tail_chain_samples < -1 ||
+      o->tail_wave_pct < 0 || o->tail_wave_pct > 1000) {
     f3g_set_error("negative option");
     return 1;
   }

@@ -127,6 +127,45 @@ int f3g_chunk_samples(const f3g_ctx *c, long long samples, int threads, int bloc
   return (int)per;
 }
 
+long long f3g_chunk_passes(F3GPass *p, int n, int threads, int blocks, int S, long long *prefix) {
+  /* the tail chunks: a quarter of S (at least 64 samples per thread), for
+   * the launch's last samples -- a fraction of one wave of S chunks -- so
+   * the blocks that took the last long chunks and those still taking short
+   * ones finish within a short chunk of each other */
+  int St = f3g_opts.tail_chain_samples > 0 ? f3g_opts.tail_chain_samples : S / 4;
+  if (f3g_opts.tail_chain_samples < 0 || S < 512 || St < 64) St = S;
+  if (St > S) St = S;
+  const double waves = f3g_opts.tail_wave_pct > 0 ? f3g_opts.tail_wave_pct / 100.0 : 0.5;
+  const long long big = (long long)threads * S, small = (long long)threads * St;
+  long long r = St < S ? (long long)(waves * blocks * (double)big) : 0;
+  for (int i = n - 1; i >= 0; i--) {
+    F3GPass *q = &p[i];
+    const long long ns = q->samples;
+    q->S = S;
+    q->S_tail = St;
+    if (r <= 0) {
+      q->chunk_tail = (ns + big - 1) / big;
+      q->nchunks = q->chunk_tail;
+    } else if (r >= ns) {
+      q->chunk_tail = 0;
+      q->nchunks = (ns + small - 1) / small;
+      r -= ns;
+    } else {
+      q->chunk_tail = (ns - r) / big;
+      q->nchunks = q->chunk_tail + (ns - q->chunk_tail * big + small - 1) / small;
+      r = 0;
+    }
+  }
+  long long tot = 0;
+  for (int i = 0; i < n; i++) {
+    p[i].chunk_begin = tot;
+    if (prefix) prefix[i] = tot;
+    tot += p[i].nchunks;
+  }
+  if (prefix) prefix[n] = tot;
+  return tot;
+}
+
 static int compute_geom(flam3_frame *spec, const flam3_genome *cp, int field, double **filter, f3g_geom *g) {
   g->oversample = cp->spatial_oversample;
   g->image_width = cp->width;
@@ -861,18 +900,12 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
       int S = f3g_chunk_samples(c, batch_samples, threads, blocks, spec->sub_batch_size);
       unsigned long long *d_counts =
           (unsigned long long *)((char *)c->d_ctr + offsetof(F3GCounters, badvals));
+      total_chunks = f3g_chunk_passes(c->h_passes, ntemporal, threads, blocks, S, c->h_prefix);
       for (int ts = 0; ts < ntemporal; ts++) {
-        F3GPass *p = &c->h_passes[ts];
-        p->S = S;
-        p->counters = d_counts;
-        p->chunk_begin = total_chunks;
-        p->nchunks = (p->samples + (long long)threads * S - 1) / ((long long)threads * S);
-        total_chunks += p->nchunks;
-        c->h_prefix[ts] = p->chunk_begin;
+        c->h_passes[ts].counters = d_counts;
         c->h_items[ts].pass = c->d_passes + ts;
         c->h_items[ts].chunk_first = 0;
       }
-      c->h_prefix[ntemporal] = total_chunks;
       int nxmax = 0;
       for (int ts = 0; ts < ntemporal; ts++)
         if (c->h_passes[ts].num_xforms > nxmax) nxmax = c->h_passes[ts].num_xforms;

@@ -49,7 +49,7 @@ enum { J_QUEUED = 0, J_ACTIVE, J_DONE, J_FAILED };
 enum { P_ITER = 0, P_TAIL, P_WAIT_UP };
 
 typedef struct {
-  int de_on, mfc, mfi, R, nk, use_count, full, mode, S;
+  int de_on, mfc, mfi, R, nk, use_count, full, mode, S, blocks;
   double k1, k2, curve;
   size_t kinfo_off; /* floats into the job's kinfo table */
   long long chunks; /* chunks of the batch (all temporal samples) */
@@ -441,19 +441,10 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
     if (occ < 1) occ = 1;
     const int blocks = f3g_opts.blocks > 0 ? f3g_opts.blocks : nsm * occ;
     b->S = force_S > 0 ? force_S : f3g_chunk_samples(NULL, batch_samples, j->threads, blocks, spec->sub_batch_size);
-    long long *pre = j->pass_prefix + (size_t)batch * (ntemporal + 1);
-    long long tot = 0;
-    const long long cs = (long long)j->threads * b->S;
-    for (int ts = 0; ts < ntemporal; ts++) {
-      F3GPass *p = &j->h_passes[batch * ntemporal + ts];
-      p->S = b->S;
-      p->nchunks = (p->samples + cs - 1) / cs;
-      p->chunk_begin = tot;
-      pre[ts] = tot;
-      tot += p->nchunks;
-    }
-    pre[ntemporal] = tot;
-    b->chunks = tot;
+    b->blocks = blocks;
+    /* the plain render's chunking, so a served job draws the same samples */
+    b->chunks = f3g_chunk_passes(&j->h_passes[batch * ntemporal], ntemporal, j->threads, blocks, b->S,
+                                 j->pass_prefix + (size_t)batch * (ntemporal + 1));
     j->total_samples += (double)batch_samples;
   }
   /* tonemap constants (render.c tail; rect.c:1069-1081) */
@@ -485,19 +476,8 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
         for (int batch = 0; batch < nbatches; batch++) {
           batch_plan *b = &j->bp[batch];
           b->S = tS;
-          long long *pre = j->pass_prefix + (size_t)batch * (ntemporal + 1);
-          long long tot = 0;
-          const long long cs = (long long)j->threads * tS;
-          for (int ts = 0; ts < ntemporal; ts++) {
-            F3GPass *p = &j->h_passes[batch * ntemporal + ts];
-            p->S = tS;
-            p->nchunks = (p->samples + cs - 1) / cs;
-            p->chunk_begin = tot;
-            pre[ts] = tot;
-            tot += p->nchunks;
-          }
-          pre[ntemporal] = tot;
-          b->chunks = tot;
+          b->chunks = f3g_chunk_passes(&j->h_passes[batch * ntemporal], ntemporal, j->threads, b->blocks, tS,
+                                       j->pass_prefix + (size_t)batch * (ntemporal + 1));
         }
       }
     }

@@ -340,6 +340,10 @@ const char *flam3gpu_version(void);
  * (each hit's channels truncated before the add, and for bits 32 the
  * log-scaled accumulator truncated too, flam3.c:3642-3647, 3688-3703,
  * 3771-3856); 1 = exact FP32 sums (more accurate than the reference).
+ * tail_chain_samples, tail_wave_pct: the last samples of each iterate launch
+ * (about half a wave of full chunks) run in chunks a quarter as long, so the
+ * blocks finish close together; the chunking is fixed when a render is
+ * planned (the same for the plain and the served render of a frame).
  * host_plan: 0 = the temporal samples of frames with several genomes
  * (animation, motion blur) are interpolated, prepared and packed on the
  * device, one block per sample; 1 = on host threads (always for one genome,
@@ -357,7 +361,9 @@ typedef struct {
   int de_stats;       /* 1: band DE counts its work (flam3gpu_last_de_work) */
   int float_buckets;  /* 1: bits 32/33 keep exact FP32 sums (no per-hit truncation) */
   int host_plan;      /* 1: plan every temporal sample on host threads (0: multi-genome frames on the device) */
-  int reserved[3];
+  int tail_chain_samples; /* samples per thread of the launch's last chunks (0: chain length / 4; -1: none) */
+  int tail_wave_pct;  /* those chunks hold this percentage of one wave of full chunks (0 = 50) */
+  int reserved[1];
 } flam3gpu_options;
 
 void flam3gpu_default_options(flam3gpu_options *o);

@@ -39,7 +39,8 @@ class F3GPass(C.Structure):
                 ("bounds", C.c_double * 4), ("rot", (C.c_double * 2) * 2), ("rot_center", C.c_double * 2),
                 ("rotate", C.c_int), ("width", C.c_int), ("height", C.c_int), ("ws0", C.c_double),
                 ("wb0s0", C.c_double), ("hs1", C.c_double), ("hb1s1", C.c_double), ("buckets", C.c_void_p),
-                ("count", C.c_void_p), ("bucket_kind", C.c_int), ("S", C.c_int), ("counters", C.c_void_p),
+                ("count", C.c_void_p), ("bucket_kind", C.c_int), ("S", C.c_int), ("S_tail", C.c_int),
+                ("chunk_tail", C.c_int64), ("counters", C.c_void_p),
                 ("xf", F3GXform * NX)]
 
 
