@@ -329,7 +329,7 @@ const char *flam3gpu_version(void);
  * with non-unity xaos always use mode 0.  iter_precision: 32 or 64 (FP64
  * iteration, slow on GB300; parity work).  threads_per_block, blocks: 0 =
  * automatic.  chain_samples: samples per chain before a restart with a new
- * random point and fuse (0 = f->sub_batch_size, like the reference).
+ * random point and fuse (at most f->sub_batch_size, like the reference).
  * de_tile: output pixels per tile edge of the fused density-estimation
  * kernel (8 .. 32; 0 = 16).  de_kernel: 0 = density estimation by owner
  * bands (register accumulators, no atomics; default), 1 = the fused tile
@@ -340,10 +340,12 @@ const char *flam3gpu_version(void);
  * (each hit's channels truncated before the add, and for bits 32 the
  * log-scaled accumulator truncated too, flam3.c:3642-3647, 3688-3703,
  * 3771-3856); 1 = exact FP32 sums (more accurate than the reference).
- * tail_chain_samples, tail_wave_pct: the last samples of each iterate launch
- * (about half a wave of full chunks) run in chunks a quarter as long, so the
- * blocks finish close together; the chunking is fixed when a render is
- * planned (the same for the plain and the served render of a frame).
+ * chain_samples 0: 1024, or 2048 when a launch holds at least 8 waves of
+ * 2048-sample chains.  tail_chain_samples, tail_wave_pct: the last samples
+ * of each iterate launch (half a wave of full chunks, a whole wave with
+ * 2048-sample chains) run in chunks a quarter as long, so the blocks finish
+ * close together; the chunking is fixed when a render is planned (the same
+ * for the plain and the served render of a frame).
  * host_plan: 0 = the temporal samples of frames with several genomes
  * (animation, motion blur) are interpolated, prepared and packed on the
  * device, one block per sample; 1 = on host threads (always for one genome,
@@ -362,7 +364,7 @@ typedef struct {
   int float_buckets;  /* 1: bits 32/33 keep exact FP32 sums (no per-hit truncation) */
   int host_plan;      /* 1: plan every temporal sample on host threads (0: multi-genome frames on the device) */
   int tail_chain_samples; /* samples per thread of the launch's last chunks (0: chain length / 4; -1: none) */
-  int tail_wave_pct;  /* those chunks hold this percentage of one wave of full chunks (0 = 50) */
+  int tail_wave_pct;  /* those chunks hold this percentage of one wave of full chunks (0: 50, 100 for 2048-sample chains) */
   int reserved[1];
 } flam3gpu_options;
 
