@@ -155,9 +155,20 @@ __device__ __forceinline__ float m_atan2(float y, float x) {
   if (x != x || y != y) r = x + y;
   return copysignf(r, y);
 }
-/* square root from the hardware reciprocal square root (about 3 ulp) */
+/* square root: the hardware approximation (PTX sqrt.approx.f32: one
+ * instruction, 0 for 0, NaN below 0); F3G_SQRT_RSQ keeps x * rsqrt(x) with
+ * the zero and negative cases selected (about 3 ulp) */
+#ifndef F3G_SQRT_RSQ
+#define F3G_SQRT_RSQ 0
+#endif
 __device__ __forceinline__ float m_sqrt(float x) {
+#if F3G_SQRT_RSQ
   return x > 0.0f ? x * rsqrtf(x) : (x == 0.0f ? 0.0f : __int_as_float(0x7fc00000));
+#else
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#endif
 }
 #else
 __device__ __forceinline__ float m_atan2(float y, float x) { return atan2f(y, x); }
@@ -183,6 +194,12 @@ __device__ __forceinline__ float m_rint(float x) { return rintf(x); }
 __device__ __forceinline__ double m_rint(double x) { return rint(x); }
 __device__ __forceinline__ float m_fabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double m_fabs(double x) { return fabs(x); }
+
+/* F3G_ANGLES_RSQ: FP32 sin and cos of the angle (x/r, y/r) from one
+ * reciprocal square root instead of two approximate divides */
+#ifndef F3G_ANGLES_RSQ
+#define F3G_ANGLES_RSQ 1
+#endif
 
 /* NaN, or |x| > 1e10 (flam3.c:269-272); the one-compare form measured
  * 1.1 % faster on the 1920x1080 still (48.9 against 48.3 Giter/s) */
@@ -218,8 +235,8 @@ template <typename R> struct Helper {
 #define P(name) x.prm[PRM_##name]
 
 /* variations 0-19 (the set the common genomes use) */
-template <typename R>
-__device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R> &x, uint32_t rword) {
+template <typename R, class G>
+__device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R> &x, G &rng) {
   switch (v) {
     case 0: f.p0 += w * f.tx; f.p1 += w * f.ty; break;
     case 1: f.p0 += w * m_sin(f.tx); f.p1 += w * m_sin(f.ty); break;
@@ -261,8 +278,9 @@ __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R>
       f.p0 += w * (m0 + m1); f.p1 += w * (m0 - m1);
     } break;
     case 13: {
+      /* julia draws one word (variations.c:350-376) */
       R a = (R)0.5 * f.atan_xy, sa, ca;
-      if (rword & 1u) a += PI_R;
+      if (rng.word() & 1u) a += PI_R;
       R r = w * m_sqrt(f.sqrtv); m_sincos(a, &sa, &ca);
       f.p0 += r * ca; f.p1 += r * sa;
     } break;
@@ -818,8 +836,18 @@ __device__ __forceinline__ bool apply_xform(const XfS<R> &x, const uint8_t *var_
   f.atan_xy = f.sina = f.cosa = f.atan_yx = (R)0;
   if (x.flags & F3G_F_ATAN_XY) f.atan_xy = m_atan2(f.tx, f.ty);
   if (x.flags & F3G_F_ANGLES) {
-    f.sina = m_div(f.tx, f.sqrtv);
-    f.cosa = m_div(f.ty, f.sqrtv);
+#if F3G_ANGLES_RSQ
+    if (sizeof(R) == 4) {
+      /* FP32: one reciprocal square root for both quotients */
+      const R r = (R)rsqrtf((float)f.sumsq);
+      f.sina = f.tx * r;
+      f.cosa = f.ty * r;
+    } else
+#endif
+    {
+      f.sina = m_div(f.tx, f.sqrtv);
+      f.cosa = m_div(f.ty, f.sqrtv);
+    }
   }
   if (x.flags & F3G_F_ATAN_YX) f.atan_yx = m_atan2(f.ty, f.tx);
   f.p0 = (R)0;
@@ -840,10 +868,8 @@ __device__ __forceinline__ bool apply_xform(const XfS<R> &x, const uint8_t *var_
                                                    f.atan_yx, f.p0, f.p1, &x, w0, w1, w2, w3, w4);
       f.p0 = r.x;
       f.p1 = r.y;
-    } else {
-      const uint32_t rw = (v == 13) ? rng.word() : 0u; /* julia draws one word */
-      var_basic<R>(v, w, f, x, rw);
-    }
+    } else
+      var_basic<R, G>(v, w, f, x, rng);
   }
   if (x.flags & F3G_F_POST) {
     qx = x.post[0] * f.p0 + x.post[2] * f.p1 + x.post[4];
