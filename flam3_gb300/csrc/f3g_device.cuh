@@ -278,7 +278,7 @@ __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R>
       f.p0 += w * (m0 + m1); f.p1 += w * (m0 - m1);
     } break;
     case 13: {
-      /* julia draws one word (variations.c:350-376) */
+      /* julia draws one word (variations.c:350-372) */
       R a = (R)0.5 * f.atan_xy, sa, ca;
       if (rng.word() & 1u) a += PI_R;
       R r = w * m_sqrt(f.sqrtv); m_sincos(a, &sa, &ca);

@@ -45,7 +45,7 @@ template <typename R> struct PassS {
   long long samples, nchunks, chunk_tail;
   unsigned long long *counters;
   uint32_t key0, key1;
-  R b0, b1, b2, b3, r00, r01, r10, r11, rcx, rcy, ws0, wb0s0, hs1, hb1s1;
+  R b0, b1, b2, b3, r00, r01, r10, r11, rcx, rcy, ws0, wb0s0, hs1, hb1s1, cmap_size_r;
   double db0, db1, db2, db3, dws0, dwb0s0, dhs1, dhb1s1;
   void *buckets, *count;
   uint16_t nbrk[F3G_MAX_XFORMS + 1];
@@ -70,7 +70,7 @@ __device__ void stage_pass(PassS<R> &s, const F3GPass *__restrict__ p) {
     s.final_enable = p->final_enable; s.chaos_enable = p->chaos_enable; s.fuse = p->fuse;
     s.mode = p->iter_mode; s.full = p->full_variations;
     s.width = p->width; s.height = p->height; s.nbuckets = p->width * p->height;
-    s.rotate = p->rotate; s.cmap_size = p->cmap_size;
+    s.rotate = p->rotate; s.cmap_size = p->cmap_size; s.cmap_size_r = (R)p->cmap_size;
     s.palette_mode = p->palette_mode; s.bucket_kind = p->bucket_kind; s.trunc = p->trunc_hits;
     s.samples = p->samples; s.nchunks = p->nchunks; s.key0 = p->key[0]; s.key1 = p->key[1];
     s.b0 = (R)p->bounds[0]; s.b1 = (R)p->bounds[1]; s.b2 = (R)p->bounds[2]; s.b3 = (R)p->bounds[3];
@@ -167,9 +167,10 @@ __device__ __forceinline__ int bucket_of(const PassS<R> &s, R qx, R qy) {
     xi = (int)(s.ws0 * (p0 - s.b0));
     yi = (int)(s.hs1 * (p1 - s.b1));
   }
-  /* inside the bounds xi <= W and yi <= H, so the index fits 32 bits */
+  /* inside the bounds xi <= W and yi <= H, so the index fits 32 bits; one
+   * unsigned compare tests 0 <= idx < nbuckets */
   const int idx = xi + s.width * yi;
-  return (idx < 0 || idx >= s.nbuckets) ? -1 : idx;
+  return (unsigned)idx >= (unsigned)s.nbuckets ? -1 : idx;
 }
 
 /* rect.c:411-516 for one sample.  With `agg` (warp-uniform), lanes of the
@@ -182,7 +183,7 @@ __device__ __forceinline__ unsigned plot(const PassS<R> &s, R qx, R qy, R qc, R 
   if (idx < 0) return 0u;
   if (qo == (R)0) return 0u;
   float4 col;
-  const R dbl_index0 = qc * (R)s.cmap_size;
+  const R dbl_index0 = qc * s.cmap_size_r;
   int ci = (int)dbl_index0;
   const int cm1 = s.cmap_size - 1;
   if (s.palette_mode == 1) {
