@@ -288,14 +288,16 @@ __device__ __forceinline__ bool chain_step(const PassS<R> &s, int fn, R &px, R &
   return true;
 }
 
-/* F3G_LEAN_RNG: 1 -- the iterate kernels' random streams read the pass key
- * and chunk index from shared memory at each refill (ChunkRng,
- * ChunkWarpWords: 24 fewer spilled bytes in mode 1); 0 (default) -- they
- * hold them in registers (Rng, WarpWords), measured 1 % faster on the
- * 1920x1080 still (48.4 against 47.9 Giter/s).  The words are the same
- * either way. */
+/* F3G_LEAN_RNG: where the iterate kernels' random streams keep their state.
+ * 0: pass key, counters and words in registers (Rng, WarpWords); 1: the
+ * pass key and chunk index in shared memory, read at each refill (ChunkRng,
+ * ChunkWarpWords); 2 (default): the words in shared memory too
+ * (ChunkRngS, ChunkWarpWordsS), one counter register per stream.  The
+ * kernel runs at its 64-register cap, so each register freed is a spill
+ * avoided: on the 1920x1080 still 50.7 (0), 51.6 (1) and 52.5 (2) Giter/s.
+ * The words are the same at every level. */
 #ifndef F3G_LEAN_RNG
-#define F3G_LEAN_RNG 0
+#define F3G_LEAN_RNG 2
 #endif
 
 /* The random streams of the chunk a block is running: the pass key and the
@@ -344,6 +346,53 @@ struct ChunkWarpWords {
   }
 };
 
+/* The same two streams with their words in shared memory as well
+ * (F3G_LEAN_RNG 2): a thread keeps one word counter.  A thread's four words
+ * sit at f3g_thread_words[k][thread] (consecutive threads, consecutive
+ * banks); a warp's 128-word block at f3g_warp_words[warp][n], lane L's four
+ * words at 4L..4L+3 -- word n of the block is component n % 4 of lane n / 4,
+ * as in ChunkWarpWords -- read as a broadcast. */
+static __shared__ __align__(16) uint32_t f3g_thread_words[4][256];
+static __shared__ __align__(16) uint32_t f3g_warp_words[8][128];
+
+struct ChunkRngS {
+  uint32_t m;
+  __device__ __forceinline__ void init() { m = 0; }
+  __device__ __forceinline__ uint32_t word() {
+    const unsigned t = threadIdx.x;
+    if ((m & 3u) == 0) {
+      const uint4 r = philox_block(f3g_chunk_ctx[2], m >> 2, t, 0x5EEDu, f3g_chunk_ctx[0], f3g_chunk_ctx[1]);
+      f3g_thread_words[0][t] = r.x;
+      f3g_thread_words[1][t] = r.y;
+      f3g_thread_words[2][t] = r.z;
+      f3g_thread_words[3][t] = r.w;
+    }
+    const uint32_t w = f3g_thread_words[m & 3u][t];
+    m++;
+    return w;
+  }
+};
+
+struct ChunkWarpWordsS {
+  uint32_t n;
+  __device__ __forceinline__ void init() { n = 0; }
+  /* warp-uniform: every lane calls it at the same step */
+  __device__ __forceinline__ uint32_t word() {
+    const unsigned warp = threadIdx.x >> 5;
+    if ((n & 127u) == 0) {
+      const unsigned lane = threadIdx.x & 31u;
+      const uint4 r = philox_block(f3g_chunk_ctx[2], n >> 7, 0xC0DE0000u | warp, lane, f3g_chunk_ctx[0],
+                                   f3g_chunk_ctx[1]);
+      __syncwarp(); /* every lane has read the last block */
+      reinterpret_cast<uint4 *>(f3g_warp_words[warp])[lane] = r;
+      __syncwarp();
+    }
+    const uint32_t w = f3g_warp_words[warp][n & 127u];
+    n++;
+    return w;
+  }
+};
+
 /* mode 0: independent chains, one per thread */
 template <typename R, bool FULL>
 __device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, long long base, long long len,
@@ -352,7 +401,11 @@ __device__ void run_chunk_thread(const PassS<R> &s, long long local_chunk, long 
   long long n_chunk = s.samples - base;
   if (n_chunk > len) n_chunk = len;
   const int q = (int)(n_chunk / T + ((long long)t < n_chunk % T ? 1 : 0));
-#if F3G_LEAN_RNG
+#if F3G_LEAN_RNG == 2
+  ChunkRngS rng;
+  rng.init();
+  typedef ChunkRngS RngT;
+#elif F3G_LEAN_RNG
   ChunkRng rng;
   rng.init();
   typedef ChunkRng RngT;
@@ -563,6 +616,12 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
 #define F3G_EXCHANGE 1
 #endif
 
+/* F3G_ROT_CLOSED: the exchange's round rotation from the round number
+ * (1) or accumulated across rounds (0) -- the same values */
+#ifndef F3G_ROT_CLOSED
+#define F3G_ROT_CLOSED 0
+#endif
+
 /* shared-memory mbarrier helpers (PTX mbarrier.*; CTA scope) */
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
@@ -636,7 +695,13 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
    * at xb + k * half */
   unsigned char *const xb = reinterpret_cast<unsigned char *>(buf);
   const unsigned half = (unsigned)(sizeof(ShufPoint<R>) * T);
-#if F3G_LEAN_RNG
+#if F3G_LEAN_RNG == 2
+  ChunkRngS rng;
+  rng.init();
+  ChunkWarpWordsS ww;
+  ww.init();
+  typedef ChunkRngS RngT;
+#elif F3G_LEAN_RNG
   ChunkRng rng;
   rng.init();
   ChunkWarpWords ww;
@@ -663,7 +728,9 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     if (lane == 0) mbar_arrive(&xc.bar[1]);
   }
   int fuse_left = 2 * s.fuse + shuffle_every;
-  uint32_t rot = 0;
+#if !F3G_ROT_CLOSED
+  uint32_t rot_acc = 0;
+#endif
   /* bucket-sharing probes: bits 0-2 probes taken, 3-5 probes with shared
    * buckets, bit 6 aggregation on */
   int agg_state = (F3G_AGG == 2 || (F3G_AGG == 1 && s.bucket_kind == F3G_BK_F64)) ? 64 : 0;
@@ -700,7 +767,14 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     /* this round's points to buffer h&1: transpose lanes across warps, XOR
      * the low five bits, rotate by whole 32-point segments (block-uniform
      * amounts), at swizzled slots (32 distinct banks) */
-    rot += 0x9E3779B1u * (uint32_t)(round + 1);
+    /* 0x9E3779B1 * (1 + 2 + ... + (h+1)), from the round (no register
+     * carried across rounds) */
+#if F3G_ROT_CLOSED
+    const uint32_t rot = 0x9E3779B1u * (((uint32_t)(round + 1) * (uint32_t)(round + 2)) >> 1);
+#else
+    rot_acc += 0x9E3779B1u * (uint32_t)(round + 1);
+    const uint32_t rot = rot_acc;
+#endif
     const int x5 = (int)(rot >> 27), kr = (int)(rot >> 24) % G;
     const int dst = (((lane * G + wl) ^ x5) + 32 * kr) & (T - 1);
     const int wslot = dst ^ ((dst >> 5) & 31);
