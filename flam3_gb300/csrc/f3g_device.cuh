@@ -195,6 +195,11 @@ __device__ __forceinline__ double m_rint(double x) { return rint(x); }
 __device__ __forceinline__ float m_fabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double m_fabs(double x) { return fabs(x); }
 
+/* F3G_LAZY_ANGLES: see var_basic */
+#ifndef F3G_LAZY_ANGLES
+#define F3G_LAZY_ANGLES 1
+#endif
+
 /* F3G_ANGLES_RSQ: FP32 sin and cos of the angle (x/r, y/r) from one
  * reciprocal square root instead of two approximate divides */
 #ifndef F3G_ANGLES_RSQ
@@ -235,8 +240,37 @@ template <typename R> struct Helper {
 #define P(name) x.prm[PRM_##name]
 
 /* variations 0-19 (the set the common genomes use) */
-template <typename R, class G>
+/* The angle terms of apply_xform (variations.c:2153-2170): atan2(tx, ty)
+ * and (sin, cos) of the point's angle as (tx/r, ty/r) -- FP32 from one
+ * reciprocal square root when F3G_ANGLES_RSQ, else two divides. */
+template <typename R> __device__ __forceinline__ R pre_atan_xy(const Helper<R> &f) { return m_atan2(f.tx, f.ty); }
+template <typename R> __device__ __forceinline__ void pre_angles(const Helper<R> &f, R &sina, R &cosa) {
+#if F3G_ANGLES_RSQ
+  if (sizeof(R) == 4) {
+    const R r = (R)rsqrtf((float)f.sumsq);
+    sina = f.tx * r;
+    cosa = f.ty * r;
+    return;
+  }
+#endif
+  sina = m_div(f.tx, f.sqrtv);
+  cosa = m_div(f.ty, f.sqrtv);
+}
+
+/* Variations 0-19.  LAZY: the angle terms are computed here, by the
+ * variations that use them, instead of once per xform by apply_xform (the
+ * same values: they live only inside the case, which matters at the
+ * iterate kernel's register cap). */
+template <typename R, class G, bool LAZY>
 __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R> &x, G &rng) {
+#define ATAN_XY (LAZY ? pre_atan_xy<R>(f) : f.atan_xy)
+#define ANGLES(sa_, ca_)          \
+  R sa_, ca_;                     \
+  if (LAZY) pre_angles<R>(f, sa_, ca_); \
+  else {                          \
+    sa_ = f.sina;                 \
+    ca_ = f.cosa;                 \
+  }
   switch (v) {
     case 0: f.p0 += w * f.tx; f.p1 += w * f.ty; break;
     case 1: f.p0 += w * m_sin(f.tx); f.p1 += w * m_sin(f.ty); break;
@@ -250,36 +284,38 @@ __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R>
       R r = m_div(w, f.sqrtv + EPS_R);
       f.p0 += (f.tx - f.ty) * (f.tx + f.ty) * r; f.p1 += (R)2.0 * f.tx * f.ty * r;
     } break;
-    case 5: f.p0 += w * (f.atan_xy * ONE_PI_R); f.p1 += w * (f.sqrtv - (R)1.0); break;
+    case 5: f.p0 += w * (ATAN_XY * ONE_PI_R); f.p1 += w * (f.sqrtv - (R)1.0); break;
     case 6: {
-      R a = f.atan_xy, r = f.sqrtv;
+      R a = ATAN_XY, r = f.sqrtv;
       f.p0 += w * r * m_sin(a + r); f.p1 += w * r * m_cos(a - r);
     } break;
     case 7: {
-      R a = f.sqrtv * f.atan_xy, sa, ca, r = w * f.sqrtv; m_sincos(a, &sa, &ca);
+      R a = f.sqrtv * ATAN_XY, sa, ca, r = w * f.sqrtv; m_sincos(a, &sa, &ca);
       f.p0 += r * sa; f.p1 += (-r) * ca;
     } break;
     case 8: {
-      R a = f.atan_xy * ONE_PI_R, r = PI_R * f.sqrtv, sr, cr; m_sincos(r, &sr, &cr);
+      R a = ATAN_XY * ONE_PI_R, r = PI_R * f.sqrtv, sr, cr; m_sincos(r, &sr, &cr);
       f.p0 += w * sr * a; f.p1 += w * cr * a;
     } break;
     case 9: {
       R r = f.sqrtv + EPS_R, r1 = m_div(w, r), sr, cr; m_sincos(r, &sr, &cr);
-      f.p0 += r1 * (f.cosa + sr); f.p1 += r1 * (f.sina - cr);
+      ANGLES(sina, cosa)
+      f.p0 += r1 * (cosa + sr); f.p1 += r1 * (sina - cr);
     } break;
-    case 10: { R r = f.sqrtv + EPS_R; f.p0 += m_div(w * f.sina, r); f.p1 += w * f.cosa * r; } break;
+    case 10: { ANGLES(sina, cosa) R r = f.sqrtv + EPS_R; f.p0 += m_div(w * sina, r); f.p1 += w * cosa * r; } break;
     case 11: {
       R sr, cr; m_sincos(f.sqrtv, &sr, &cr);
-      f.p0 += w * f.sina * cr; f.p1 += w * f.cosa * sr;
+      ANGLES(sina, cosa)
+      f.p0 += w * sina * cr; f.p1 += w * cosa * sr;
     } break;
     case 12: {
-      R a = f.atan_xy, r = f.sqrtv, n0 = m_sin(a + r), n1 = m_cos(a - r);
+      R a = ATAN_XY, r = f.sqrtv, n0 = m_sin(a + r), n1 = m_cos(a - r);
       R m0 = n0 * n0 * n0 * r, m1 = n1 * n1 * n1 * r;
       f.p0 += w * (m0 + m1); f.p1 += w * (m0 - m1);
     } break;
     case 13: {
       /* julia draws one word (variations.c:350-372) */
-      R a = (R)0.5 * f.atan_xy, sa, ca;
+      R a = (R)0.5 * ATAN_XY, sa, ca;
       if (rng.word() & 1u) a += PI_R;
       R r = w * m_sqrt(f.sqrtv); m_sincos(a, &sa, &ca);
       f.p0 += r * ca; f.p1 += r * sa;
@@ -306,11 +342,14 @@ __device__ __forceinline__ void var_basic(int v, R w, Helper<R> &f, const XfS<R>
       f.p0 += dx * cdy; f.p1 += dx * sdy;
     } break;
     case 19: {
-      R r = w * m_pow(f.sqrtv, f.sina);
-      f.p0 += r * f.cosa; f.p1 += r * f.sina;
+      ANGLES(sina, cosa)
+      R r = w * m_pow(f.sqrtv, sina);
+      f.p0 += r * cosa; f.p1 += r * sina;
     } break;
     default: break;
   }
+#undef ATAN_XY
+#undef ANGLES
 }
 
 /* variations 20-98 */
@@ -834,22 +873,13 @@ __device__ __forceinline__ bool apply_xform(const XfS<R> &x, const uint8_t *var_
   f.sumsq = f.tx * f.tx + f.ty * f.ty;
   f.sqrtv = m_sqrt(f.sumsq);
   f.atan_xy = f.sina = f.cosa = f.atan_yx = (R)0;
-  if (x.flags & F3G_F_ATAN_XY) f.atan_xy = m_atan2(f.tx, f.ty);
-  if (x.flags & F3G_F_ANGLES) {
-#if F3G_ANGLES_RSQ
-    if (sizeof(R) == 4) {
-      /* FP32: one reciprocal square root for both quotients */
-      const R r = (R)rsqrtf((float)f.sumsq);
-      f.sina = f.tx * r;
-      f.cosa = f.ty * r;
-    } else
-#endif
-    {
-      f.sina = m_div(f.tx, f.sqrtv);
-      f.cosa = m_div(f.ty, f.sqrtv);
-    }
+  /* with variations 0-19 only (FULL false) and F3G_LAZY_ANGLES, the angle
+   * terms are computed by the variations that use them */
+  if (FULL || !F3G_LAZY_ANGLES) {
+    if (x.flags & F3G_F_ATAN_XY) f.atan_xy = pre_atan_xy<R>(f);
+    if (x.flags & F3G_F_ANGLES) pre_angles<R>(f, f.sina, f.cosa);
+    if (x.flags & F3G_F_ATAN_YX) f.atan_yx = m_atan2(f.ty, f.tx);
   }
-  if (x.flags & F3G_F_ATAN_YX) f.atan_yx = m_atan2(f.ty, f.tx);
   f.p0 = (R)0;
   f.p1 = (R)0;
   for (int k = 0; k < x.nvars; k++) {
@@ -869,7 +899,7 @@ __device__ __forceinline__ bool apply_xform(const XfS<R> &x, const uint8_t *var_
       f.p0 = r.x;
       f.p1 = r.y;
     } else
-      var_basic<R, G>(v, w, f, x, rng);
+      var_basic<R, G, !FULL && F3G_LAZY_ANGLES>(v, w, f, x, rng);
   }
   if (x.flags & F3G_F_POST) {
     qx = x.post[0] * f.p0 + x.post[2] * f.p1 + x.post[4];
