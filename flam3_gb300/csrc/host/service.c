@@ -49,7 +49,7 @@ enum { J_QUEUED = 0, J_ACTIVE, J_DONE, J_FAILED };
 enum { P_ITER = 0, P_TAIL, P_WAIT_UP };
 
 typedef struct {
-  int de_on, mfc, mfi, R, nk, use_count, full, mode, S, blocks;
+  int de_on, mfc, mfi, R, nk, use_count, full, mode, S, S_tail, blocks;
   double k1, k2, curve;
   size_t kinfo_off; /* floats into the job's kinfo table */
   long long chunks; /* chunks of the batch (all temporal samples) */
@@ -73,7 +73,8 @@ typedef struct f3g_job {
   int fused_de, fused_log, need_acc, count_any, tile, band_de;
   int aborted; /* the progress callback asked to abort: no more rounds, no tail, output untouched */
   double sort_key; /* the round's ordering key (cfg.order 1 and 2) */
-  F3GPass *h_passes;      /* nbatches * ntemporal */
+  F3GPass *h_passes;      /* nbatches * ntemporal (freed once uploaded) */
+  long long *pass_tail;   /* each pass's first short chunk (F3GPass.chunk_tail), kept for round building */
   long long *pass_prefix; /* per batch: ntemporal+1 chunk offsets, concatenated */
   batch_plan *bp;
   float *h_kinfo;
@@ -271,6 +272,8 @@ static void tune_store(const char *key, int S, int tile) {
 
 static void job_free_plan(f3g_job *j) {
   free(j->h_passes);
+  free(j->pass_tail);
+  j->pass_tail = NULL;
   free(j->pass_prefix);
   free(j->bp);
   free(j->h_kinfo);
@@ -347,11 +350,12 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
   j->precision = f3g_opts.iter_precision == 64 ? 64 : 32;
   const int npass = nbatches * ntemporal;
   j->h_passes = (F3GPass *)calloc((size_t)npass, sizeof(F3GPass));
+  j->pass_tail = (long long *)calloc((size_t)npass, sizeof(long long));
   j->pass_prefix = (long long *)calloc((size_t)nbatches * (ntemporal + 1), sizeof(long long));
   j->bp = (batch_plan *)calloc((size_t)nbatches, sizeof(batch_plan));
   j->h_filter = (float *)malloc(F3G_FILTER_FLOATS(g.filter_width) * sizeof(float));
   info = (f3g_pass_info *)calloc((size_t)ntemporal, sizeof(f3g_pass_info));
-  if (!j->h_passes || !j->pass_prefix || !j->bp || !j->h_filter || !info) {
+  if (!j->h_passes || !j->pass_tail || !j->pass_prefix || !j->bp || !j->h_filter || !info) {
     f3g_set_error("host memory exhausted");
     goto done;
   }
@@ -483,6 +487,11 @@ static int plan_job(f3g_job *j, int nsm, int use_tuning, int force_S, int force_
     }
   }
   if (force_tile > 0) j->tile = force_tile;
+  /* the chunking the rounds need after the host passes are gone */
+  for (int b = 0; b < nbatches; b++) {
+    j->bp[b].S_tail = j->h_passes[b * ntemporal].S_tail;
+    for (int ts = 0; ts < ntemporal; ts++) j->pass_tail[b * ntemporal + ts] = j->h_passes[b * ntemporal + ts].chunk_tail;
+  }
   int de_any = 0, bands_ok = 1;
   for (int b = 0; b < nbatches; b++)
     if (j->bp[b].de_on) {
@@ -1160,7 +1169,19 @@ typedef struct {
   F3GItem it;
   long long span;
   int cls;
+  long long clen; /* samples per chunk of the item's chunks */
 } tmp_item;
+
+/* a round's work list: by kernel class, then longest chunks first, so each
+ * class's launch ends on short chunks and its blocks finish close together
+ * (the jobs of a round complete with the round, so the order within it
+ * changes no job's latency) */
+static int tmp_item_cmp(const void *a, const void *b) {
+  const tmp_item *x = (const tmp_item *)a, *y = (const tmp_item *)b;
+  if (x->cls != y->cls) return x->cls - y->cls;
+  if (x->clen != y->clen) return x->clen > y->clen ? -1 : 1;
+  return 0;
+}
 
 static void round_done(flam3gpu_service *s, round_buf *r);
 
@@ -1243,7 +1264,10 @@ static int issue_round(flam3gpu_service *s) {
     int p = j->pass_hint;
     while (pre[p + 1] <= cur) p++;
     while (cur < end) {
-      const long long stop = pre[p + 1] < end ? pre[p + 1] : end;
+      long long stop = pre[p + 1] < end ? pre[p + 1] : end;
+      /* items do not straddle the pass's switch to short chunks */
+      const long long tail_at = pre[p] + j->pass_tail[(size_t)j->batch * j->ntemporal + p];
+      if (b->S_tail > 0 && cur < tail_at && stop > tail_at) stop = tail_at;
       if (stop > cur) {
         if (nit == cap) {
           cap *= 2;
@@ -1259,6 +1283,7 @@ static int issue_round(flam3gpu_service *s) {
         ti[nit].it.chunk_first = cur - pre[p];
         ti[nit].span = stop - cur;
         ti[nit].cls = b->full * 2 + b->mode;
+        ti[nit].clen = (long long)j->threads * (b->S_tail > 0 && cur >= tail_at ? b->S_tail : b->S);
         nit++;
         cur = stop;
       }
@@ -1290,6 +1315,7 @@ static int issue_round(flam3gpu_service *s) {
     free(takes);
     return 0;
   }
+  qsort(ti, nit, sizeof(tmp_item), tmp_item_cmp);
   /* classes in order; class c's prefix has one extra entry for its end */
   size_t cls_n[NCLASS] = {0}, cls_off[NCLASS + 1];
   long long tot[NCLASS] = {0};
