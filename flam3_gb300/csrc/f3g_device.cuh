@@ -220,7 +220,8 @@ template <typename R> __device__ __forceinline__ bool badvalue(R x) {
 }
 
 /* One xform staged in shared memory in the iteration precision. */
-template <typename R> struct XfS {
+/* 16-byte aligned: apply_xform loads its FP32 fields as vectors */
+template <typename R> struct __align__(16) XfS {
   R c[6], post[6];
   R color, color_speed, vis_adjusted, opacity, preblur;
   int flags, var_off, nvars;
@@ -849,6 +850,46 @@ __device__ __noinline__ typename Vec2<R>::T var_extended_impl(int v, R w, R tx, 
   return r;
 }
 
+/* The fields apply_xform reads first.  In FP32 they come in four vector
+ * loads from the 16-byte aligned record in shared memory (c[0..3],
+ * c[4..5]; color, color_speed, vis_adjusted, opacity; preblur, flags,
+ * var_off, nvars) instead of twelve scalar ones. */
+template <typename R> struct XfHead {
+  R c0, c1, c2, c3, c4, c5, color, color_speed, vis_adjusted;
+  int flags, var_off, nvars;
+};
+template <typename R> __device__ __forceinline__ void load_head(const XfS<R> &x, XfHead<R> &h) {
+  h.c0 = x.c[0]; h.c1 = x.c[1]; h.c2 = x.c[2]; h.c3 = x.c[3]; h.c4 = x.c[4]; h.c5 = x.c[5];
+  h.color = x.color; h.color_speed = x.color_speed; h.vis_adjusted = x.vis_adjusted;
+  h.flags = x.flags; h.var_off = x.var_off; h.nvars = x.nvars;
+}
+template <> __device__ __forceinline__ void load_head<float>(const XfS<float> &x, XfHead<float> &h) {
+  static_assert(offsetof(XfS<float>, c) == 0 && offsetof(XfS<float>, color) == 48 &&
+                    offsetof(XfS<float>, preblur) == 64 && offsetof(XfS<float>, flags) == 68 &&
+                    offsetof(XfS<float>, var_off) == 72 && offsetof(XfS<float>, nvars) == 76,
+                "XfS<float> layout");
+  const float4 a = *reinterpret_cast<const float4 *>(&x.c[0]);
+  const float2 b = *reinterpret_cast<const float2 *>(&x.c[4]);
+  const float4 m = *reinterpret_cast<const float4 *>(&x.color);
+  const int4 q = *reinterpret_cast<const int4 *>(&x.preblur);
+  h.c0 = a.x; h.c1 = a.y; h.c2 = a.z; h.c3 = a.w; h.c4 = b.x; h.c5 = b.y;
+  h.color = m.x; h.color_speed = m.y; h.vis_adjusted = m.z;
+  h.flags = q.y; h.var_off = q.z; h.nvars = q.w;
+}
+/* the post-transform, as two vector loads in FP32 (post[0..1], post[2..5]) */
+template <typename R>
+__device__ __forceinline__ void load_post(const XfS<R> &x, R &p0, R &p1, R &p2, R &p3, R &p4, R &p5) {
+  p0 = x.post[0]; p1 = x.post[1]; p2 = x.post[2]; p3 = x.post[3]; p4 = x.post[4]; p5 = x.post[5];
+}
+template <>
+__device__ __forceinline__ void load_post<float>(const XfS<float> &x, float &p0, float &p1, float &p2, float &p3,
+                                                 float &p4, float &p5) {
+  static_assert(offsetof(XfS<float>, post) == 24, "XfS<float> layout");
+  const float2 a = *reinterpret_cast<const float2 *>(&x.post[0]);
+  const float4 b = *reinterpret_cast<const float4 *>(&x.post[2]);
+  p0 = a.x; p1 = a.y; p2 = b.x; p3 = b.y; p4 = b.z; p5 = b.w;
+}
+
 /* variations.c:2129-2399.  p = (x, y, color); q receives (x, y, color,
  * opacity).  Returns true when the result was a bad value and was replaced
  * by a random point. */
@@ -856,12 +897,14 @@ template <typename R, bool FULL, class G>
 __device__ __forceinline__ bool apply_xform(const XfS<R> &x, const uint8_t *var_id, const R *var_w, R px, R py,
                                             R pc, R &qx, R &qy, R &qc, R &qo, G &rng) {
   Helper<R> f;
-  R s1 = x.color_speed;
-  qc = s1 * x.color + ((R)1.0 - s1) * pc;
-  qo = x.vis_adjusted;
-  f.tx = x.c[0] * px + x.c[2] * py + x.c[4];
-  f.ty = x.c[1] * px + x.c[3] * py + x.c[5];
-  if (FULL && (x.flags & F3G_F_PREBLUR)) {
+  XfHead<R> h;
+  load_head<R>(x, h);
+  R s1 = h.color_speed;
+  qc = s1 * h.color + ((R)1.0 - s1) * pc;
+  qo = h.vis_adjusted;
+  f.tx = h.c0 * px + h.c2 * py + h.c4;
+  f.ty = h.c1 * px + h.c3 * py + h.c5;
+  if (FULL && (h.flags & F3G_F_PREBLUR)) {
     /* var67_pre_blur (variations.c:1480-1496) */
     R g1 = u01<R>(rng.word()), g2 = u01<R>(rng.word()), g3 = u01<R>(rng.word()), g4 = u01<R>(rng.word());
     R rndG = x.preblur * (g1 + g2 + g3 + g4 - (R)2.0);
@@ -876,15 +919,15 @@ __device__ __forceinline__ bool apply_xform(const XfS<R> &x, const uint8_t *var_
   /* with variations 0-19 only (FULL false) and F3G_LAZY_ANGLES, the angle
    * terms are computed by the variations that use them */
   if (FULL || !F3G_LAZY_ANGLES) {
-    if (x.flags & F3G_F_ATAN_XY) f.atan_xy = pre_atan_xy<R>(f);
-    if (x.flags & F3G_F_ANGLES) pre_angles<R>(f, f.sina, f.cosa);
-    if (x.flags & F3G_F_ATAN_YX) f.atan_yx = m_atan2(f.ty, f.tx);
+    if (h.flags & F3G_F_ATAN_XY) f.atan_xy = pre_atan_xy<R>(f);
+    if (h.flags & F3G_F_ANGLES) pre_angles<R>(f, f.sina, f.cosa);
+    if (h.flags & F3G_F_ATAN_YX) f.atan_yx = m_atan2(f.ty, f.tx);
   }
   f.p0 = (R)0;
   f.p1 = (R)0;
-  for (int k = 0; k < x.nvars; k++) {
-    int v = var_id[x.var_off + k];
-    R w = var_w[x.var_off + k];
+  for (int k = 0; k < h.nvars; k++) {
+    int v = var_id[h.var_off + k];
+    R w = var_w[h.var_off + k];
     if (FULL && v >= 20) {
       /* draw this variation's words first, in its order, then call it */
       const int nd = ext_draws(v);
@@ -901,9 +944,11 @@ __device__ __forceinline__ bool apply_xform(const XfS<R> &x, const uint8_t *var_
     } else
       var_basic<R, G, !FULL && F3G_LAZY_ANGLES>(v, w, f, x, rng);
   }
-  if (x.flags & F3G_F_POST) {
-    qx = x.post[0] * f.p0 + x.post[2] * f.p1 + x.post[4];
-    qy = x.post[1] * f.p0 + x.post[3] * f.p1 + x.post[5];
+  if (h.flags & F3G_F_POST) {
+    R p0, p1, p2, p3, p4, p5;
+    load_post<R>(x, p0, p1, p2, p3, p4, p5);
+    qx = p0 * f.p0 + p2 * f.p1 + p4;
+    qy = p1 * f.p0 + p3 * f.p1 + p5;
   } else {
     qx = f.p0;
     qy = f.p1;
