@@ -346,7 +346,7 @@ def run_gpu(args):
                         "one render after one warm-up"}
     cb = None
     if world == 1 and not args.no_cpu:
-        cb, _ = cpu_baseline(steps=1)
+        cb, _ = cpu_baseline(steps=3)
     tail_ms = 1e3 * tail_s / args.steps
     tail_roof = {"bound": "hbm", "kernel": "DE + filter + tonemap (k_de_classify, k_de_bands, k_log_filter_strip "
                  "over the accumulator)", "achieved": tail_gbs, "peak": hbm_peak, "unit": "GB/s",
