@@ -190,3 +190,23 @@ def test_render_of_parsed_genome_close_to_oracle(gpulib):
     g, _ = render.render(gm.Frame(G, bits=33, seed="xml-g"))
     assert o.mean() > 5.0
     assert mae(o, g) < 2.5
+
+
+@pytest.mark.parametrize("threads", [32, 64, 128])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_block_sizes_render_like_the_default(gpulib, hq_reference, threads, mode):
+    """Blocks of 32, 64 or 128 threads (the point exchange between warps, its
+    buffers and barrier counts all depend on the block): the same samples
+    counted, the same error against the 16x render as 256-thread blocks."""
+    errs, iters = {}, {}
+    for t in (256, threads):
+        render.set_options(iter_mode=mode, threads_per_block=t)
+        try:
+            F = gm.Frame(cfg0(q=200.0), bits=33, seed="blk-%d" % t)
+            out, st = render.render(F)
+        finally:
+            render.reset_options()
+        errs[t] = mae(out, hq_reference)
+        iters[t] = st.num_iters
+    assert iters[threads] == iters[256]
+    assert errs[threads] <= 1.05 * errs[256] + 0.03, errs
