@@ -218,7 +218,7 @@ extern "C" int flam3gpu_render_noalloc(flam3_frame *spec, void *out, int field, 
       stats->num_iters += batch_size;
       p->samples = (long long)batch_size;
       p->fuse = spec->earlyclip ? 100 : 15;
-      p->iter_mode = (cp.chaos_enable || f3g_opts.iter_mode == 0) ? 0 : 1;
+      p->iter_mode = f3g_choice_mode(cp.chaos_enable);
       p->bucket_kind = bkind;
       p->trunc_hits = bits <= 33 && !f3g_opts.float_buckets;
       p->buckets = d_hist;

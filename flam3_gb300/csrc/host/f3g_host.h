@@ -144,6 +144,9 @@ int f3g_ensure(void **ptr, size_t *cap, size_t need);
 extern flam3gpu_options f3g_opts;
 /* samples per thread per chunk for a pass of `samples` samples */
 int f3g_chunk_samples(const f3g_ctx *c, long long samples, int threads, int blocks, int sub_batch_size);
+/* the xform-choice mode of a pass: 1 (warp-coherent) unless the genome has
+ * xaos, the options ask for 0, or blocks hold fewer than 4 warps */
+int f3g_choice_mode(int chaos_enable);
 /* chunking of one launch's passes (S, S_tail, chunk_tail, nchunks,
  * chunk_begin; prefix[0..n] if not NULL); returns the launch's chunks */
 long long f3g_chunk_passes(F3GPass *p, int n, int threads, int blocks, int S, long long *prefix);

@@ -172,6 +172,15 @@ long long f3g_chunk_passes(F3GPass *p, int n, int threads, int blocks, int S, lo
   return tot;
 }
 
+int f3g_choice_mode(int chaos_enable) {
+  /* mode 1 shares each step's xform draw within a warp and relies on the
+   * exchange between a block's warps to decorrelate the chains: with fewer
+   * than 4 warps per block there is too little to exchange with, so those
+   * blocks draw per thread (as for genomes with xaos) */
+  const int threads = f3g_opts.threads_per_block > 0 ? f3g_opts.threads_per_block : 256;
+  return (chaos_enable || f3g_opts.iter_mode == 0 || threads < 128) ? 0 : 1;
+}
+
 static int compute_geom(flam3_frame *spec, const flam3_genome *cp, int field, double **filter, f3g_geom *g) {
   g->oversample = cp->spatial_oversample;
   g->image_width = cp->width;
@@ -344,7 +353,7 @@ static void build_one_pass(const pass_job *pj, int ts) {
   in->batch_size = nsamples / (pj->nbatches * pj->ntemporal);
   p->samples = (long long)in->batch_size;
   p->fuse = spec->earlyclip ? 100 : 15;
-  p->iter_mode = (cp.chaos_enable || f3g_opts.iter_mode == 0) ? 0 : 1;
+  p->iter_mode = f3g_choice_mode(cp.chaos_enable);
   in->vibrancy = cp.vibrancy;
   in->gamma = cp.gamma;
   for (int k = 0; k < 3; k++) in->background[k] = cp.background[k];
@@ -614,7 +623,7 @@ static int build_batch_passes_device(f3g_ctx *c, flam3_frame *spec, int field, c
     in->batch_size = nsamples / (nbatches * ntemporal);
     p->samples = (long long)in->batch_size;
     p->fuse = spec->earlyclip ? 100 : 15;
-    p->iter_mode = (p->chaos_enable || f3g_opts.iter_mode == 0) ? 0 : 1;
+    p->iter_mode = f3g_choice_mode(p->chaos_enable);
     for (int j = 0; j < 256; j++)
       if (sg.palette[j].color[3] != 1.0) in->need_count = 1;
     in->vibrancy = sg.vibrancy;

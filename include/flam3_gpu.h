@@ -323,10 +323,11 @@ const char *flam3gpu_version(void);
 /* Execution options (no counterpart in the reference; defaults are chosen by
  * the library).  iter_mode: 0 = one independent chain per thread, xform picked
  * per thread (the reference's semantics); 1 = warp-coherent xform choice with
- * a block-wide point shuffle every `shuffle_every` steps (default, every 3
- * steps: the image error against a 16x-quality render is within 0.2 % of
- * mode 0's).  Genomes
- * with non-unity xaos always use mode 0.  iter_precision: 32 or 64 (FP64
+ * a point exchange between the block's warps every `shuffle_every` steps
+ * (default, every 3 steps: the image error against a 16x-quality render is
+ * within 0.2 % of mode 0's).  Genomes with non-unity xaos, and blocks of
+ * fewer than 128 threads (too few warps to exchange with), always use mode
+ * 0.  iter_precision: 32 or 64 (FP64
  * iteration, slow on GB300; parity work).  threads_per_block, blocks: 0 =
  * automatic.  chain_samples: samples per chain before a restart with a new
  * random point and fuse (at most f->sub_batch_size, like the reference).
