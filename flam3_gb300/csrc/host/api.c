@@ -200,6 +200,34 @@ out:
   return rc;
 }
 
+int flam3gpu_chunk_plan(const long long *samples, int n, int threads, int blocks, int sub_batch_size, int *S,
+                        int *S_tail, long long *chunk_tail, long long *nchunks) {
+  f3g_clear_error();
+  if (!samples || n < 1 || threads < 1 || blocks < 1 || !S || !S_tail || !chunk_tail || !nchunks) {
+    f3g_set_error("bad arguments to flam3gpu_chunk_plan");
+    return 1;
+  }
+  F3GPass *p = (F3GPass *)calloc((size_t)n, sizeof(F3GPass));
+  if (!p) {
+    f3g_set_error("host memory exhausted");
+    return 1;
+  }
+  long long total = 0;
+  for (int i = 0; i < n; i++) {
+    p[i].samples = samples[i];
+    total += samples[i];
+  }
+  *S = f3g_chunk_samples(NULL, total, threads, blocks, sub_batch_size);
+  f3g_chunk_passes(p, n, threads, blocks, *S, NULL);
+  *S_tail = p[0].S_tail;
+  for (int i = 0; i < n; i++) {
+    chunk_tail[i] = p[i].chunk_tail;
+    nchunks[i] = p[i].nchunks;
+  }
+  free(p);
+  return 0;
+}
+
 int flam3gpu_choice_breakpoints(const double *d, const double *c, int nstd, int nx, int walk, uint16_t *brk,
                                 int *nbrk, int *moves) {
   f3g_clear_error();

@@ -79,6 +79,9 @@ def load():
                                             C.POINTER(C.c_long), C.c_int]
     lib.flam3gpu_xform_choice_table.argtypes = [G, C.POINTER(C.c_uint16), C.POINTER(C.c_int)]
     lib.flam3gpu_plan_passes.argtypes = [F, C.c_int, C.c_void_p, C.c_int]
+    lp = C.POINTER(C.c_longlong)
+    ip = C.POINTER(C.c_int)
+    lib.flam3gpu_chunk_plan.argtypes = [lp, C.c_int, C.c_int, C.c_int, C.c_int, ip, ip, lp, lp]
     lib.flam3gpu_choice_breakpoints.argtypes = [dp, dp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint16),
                                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.flam3gpu_pass_bytes.restype = C.c_size_t
@@ -242,6 +245,19 @@ def iterate_chains(genome, starts, n, fuse, seed, precision=64):
                                    C.byref(bad), precision):
         _err(lib, "iterate_chains")
     return out, bad.value
+
+
+def chunk_plan(samples, threads=256, blocks=608, sub_batch_size=10000):
+    """The iterate launch's chunking on the host: (S, S_tail, chunk_tail,
+    nchunks) for passes of the given sample counts."""
+    lib = load()
+    n = len(samples)
+    smp = (C.c_longlong * n)(*[int(x) for x in samples])
+    S, St = C.c_int(0), C.c_int(0)
+    ct, nc = (C.c_longlong * n)(), (C.c_longlong * n)()
+    if lib.flam3gpu_chunk_plan(smp, n, threads, blocks, sub_batch_size, C.byref(S), C.byref(St), ct, nc):
+        _err(lib, "chunk_plan")
+    return S.value, St.value, list(ct), list(nc)
 
 
 def choice_breakpoints(weights, chaos=None, nstd=None, walk=False, moves=False):

@@ -64,6 +64,15 @@ int flam3gpu_apply_xform(flam3_genome *cp, int fn, int n, const double *p_in,
  * entries and receives the row count in *rows. */
 int flam3gpu_xform_choice_table(flam3_genome *cp, uint16_t *table, int *rows);
 
+/* Host probe of the iterate launch's chunking (no GPU): for passes of
+ * samples[0..n) in one launch of `blocks` blocks of `threads`, the chain
+ * length S the render picks (f->sub_batch_size as sub_batch_size), the
+ * short-chunk length S_tail, and per pass the first short chunk and the chunk
+ * count.  Chunk c of pass i holds threads*S samples below chunk_tail[i],
+ * threads*S_tail from there (the last one fewer). */
+int flam3gpu_chunk_plan(const long long *samples, int n, int threads, int blocks, int sub_batch_size, int *S,
+                        int *S_tail, long long *chunk_tail, long long *nchunks);
+
 /* Host probe of one choice row (no GPU): the breakpoints of the row with
  * xform weights d[0..nx) (times the row's chaos entries c[0..nstd), or c NULL
  * for the raw-weight row), built by the reference's 16384-step loop
