@@ -39,6 +39,11 @@ namespace f3g {
 #define F3G_FINAL_UNROLL 1
 #endif
 
+/* F3G_PRETRUNC: see stage_pass */
+#ifndef F3G_PRETRUNC
+#define F3G_PRETRUNC 1
+#endif
+
 template <typename R> struct PassS {
   int num_xforms, num_std, final_index, final_enable, chaos_enable, fuse, mode, full;
   int width, height, nbuckets, rotate, cmap_size, palette_mode, bucket_kind, S, S_tail, trunc;
@@ -65,13 +70,24 @@ template <typename R> struct ShufPoint { R x, y, c; int consec; };
 template <typename R>
 __device__ void stage_pass(PassS<R> &s, const F3GPass *__restrict__ p) {
   const int t = threadIdx.x, T = blockDim.x;
+#if F3G_PRETRUNC
+  /* integer buckets with a step palette where every xform plots at opacity
+   * 1: each hit adds a colour-map entry as it stands, so the map is
+   * truncated once here instead of at every hit (trunc 2) */
+  int vis1 = 1;
+  for (int i = t; i < p->num_xforms; i += T) vis1 &= p->xf[i].vis_adjusted == 1.0;
+  const bool pretrunc = __syncthreads_and(vis1) && p->trunc_hits && p->palette_mode == 0;
+#else
+  const bool pretrunc = false;
+#endif
   if (t == 0) {
     s.num_xforms = p->num_xforms; s.num_std = p->num_std; s.final_index = p->final_index;
     s.final_enable = p->final_enable; s.chaos_enable = p->chaos_enable; s.fuse = p->fuse;
     s.mode = p->iter_mode; s.full = p->full_variations;
     s.width = p->width; s.height = p->height; s.nbuckets = p->width * p->height;
     s.rotate = p->rotate; s.cmap_size = p->cmap_size; s.cmap_size_r = (R)p->cmap_size;
-    s.palette_mode = p->palette_mode; s.bucket_kind = p->bucket_kind; s.trunc = p->trunc_hits;
+    s.palette_mode = p->palette_mode; s.bucket_kind = p->bucket_kind;
+    s.trunc = p->trunc_hits ? (pretrunc ? 2 : 1) : 0;
     s.samples = p->samples; s.nchunks = p->nchunks; s.key0 = p->key[0]; s.key1 = p->key[1];
     s.b0 = (R)p->bounds[0]; s.b1 = (R)p->bounds[1]; s.b2 = (R)p->bounds[2]; s.b3 = (R)p->bounds[3];
     s.db0 = p->bounds[0]; s.db1 = p->bounds[1]; s.db2 = p->bounds[2]; s.db3 = p->bounds[3];
@@ -104,8 +120,11 @@ __device__ void stage_pass(PassS<R> &s, const F3GPass *__restrict__ p) {
     s.var_id[i] = p->var_id[i];
     s.var_w[i] = (R)p->var_w[i];
   }
-  for (int i = t; i < 256; i += T)
-    s.dmap[i] = make_float4(p->dmap[i][0], p->dmap[i][1], p->dmap[i][2], p->dmap[i][3]);
+  for (int i = t; i < 256; i += T) {
+    float4 d = make_float4(p->dmap[i][0], p->dmap[i][1], p->dmap[i][2], p->dmap[i][3]);
+    if (pretrunc) d = make_float4(truncf(d.x), truncf(d.y), truncf(d.z), truncf(d.w));
+    s.dmap[i] = d;
+  }
   /* xform scalars and parameters */
   const int per = 6 + 6 + 5 + PRM_COUNT;
   for (int i = t; i < nx * per; i += T) {
@@ -205,8 +224,9 @@ __device__ __forceinline__ unsigned plot(const PassS<R> &s, R qx, R qy, R qc, R 
     col.x *= o; col.y *= o; col.z *= o; col.w *= o;
     cnt *= o;
   }
-  if (s.trunc) {
-    /* integer buckets: the reference adds (unsigned)(delta) per hit */
+  if (s.trunc == 1) {
+    /* integer buckets: the reference adds (unsigned)(delta) per hit (trunc
+     * 2: the colour map is truncated already and every opacity is 1) */
     col = make_float4(truncf(col.x), truncf(col.y), truncf(col.z), truncf(col.w));
     cnt = truncf(cnt);
   }
