@@ -657,8 +657,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 /* waits for the completion of the barrier's phase of parity `ph`; false when
- * it has not completed within about two seconds (a lost arrival) */
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned ph) {
+ * it has not completed within limit_ns (a lost arrival) */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned ph, unsigned long long limit_ns) {
   const unsigned a = smem_addr(bar);
   unsigned long long t0 = 0;
   for (unsigned i = 0; i < (1u << 30); i++) {
@@ -672,7 +672,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned ph) {
     if ((i & 255) == 0) {
       const unsigned long long t = global_ns();
       if (i == 0) t0 = t;
-      else if (t - t0 > 2000000000ull) return false;
+      else if (t - t0 > limit_ns) return false;
     }
   }
   return false;
@@ -705,7 +705,7 @@ struct Exchange {
 template <typename R, bool FULL>
 __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchange &xc, unsigned &ph,
                                    long long local_chunk, long long base, long long len, int shuffle_every,
-                                   unsigned &bad_total, unsigned &hits) {
+                                   int stall, unsigned &bad_total, unsigned &hits) {
   const int T = blockDim.x, t = threadIdx.x, lane = t & 31, G = T >> 5, wl = t >> 5;
   long long n_chunk = s.samples - base;
   if (n_chunk > len) n_chunk = len;
@@ -773,7 +773,8 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     const int cur = round & 1, prev = cur ^ 1;
     /* the points of round h-1 (the warp decides together, so a wait that
      * ends at the time limit in one lane ends the exchange for all) */
-    if (!__all_sync(0xffffffffu, mbar_wait(&xc.bar[prev], (ph >> prev) & 1u))) {
+    /* every wait ends within 2 s (20 ms in the stall test) */
+    if (!__all_sync(0xffffffffu, mbar_wait(&xc.bar[prev], (ph >> prev) & 1u, stall ? 20000000ull : 2000000000ull))) {
       xc.abort = 1;
       ok_all = false;
       break;
@@ -803,7 +804,9 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     reinterpret_cast<int *>(W + 3 * T)[wslot] = consec;
     const unsigned ndone = __popc(__ballot_sync(0xffffffffu, remaining == 0 && fuse_left == 0));
     __syncwarp();
-    if (lane == 0) {
+    /* the stall test: warp 0 withholds its arrival of round 2, so every
+     * warp's wait for that round runs out */
+    if (lane == 0 && !(stall && wl == 0 && round == 2)) {
       if (ndone) atomicAdd(&xc.done[round & 3], (int)ndone);
       mbar_arrive(&xc.bar[cur]);
     }
@@ -857,11 +860,14 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GI
   __shared__ int sh_item;
 #if F3G_EXCHANGE == 1
   __shared__ Exchange xc;
+  __shared__ int sh_stall;
   unsigned ph = 0; /* phase parities of xc.bar[0..1] */
+  int stall = 1;   /* the stall test applies to block 0's first chunk only */
   if (MODE == 1 && threadIdx.x == 0) {
     mbar_init(&xc.bar[0], blockDim.x >> 5);
     mbar_init(&xc.bar[1], blockDim.x >> 5);
     xc.abort = 0;
+    sh_stall = blockIdx.x == 0 && ctr->test_stall != 0;
   }
 #endif
   int cur = -1;
@@ -917,7 +923,11 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GI
       len = TT * s.S_tail;
     }
 #if F3G_EXCHANGE == 1
-    if (MODE == 1) (void)run_chunk_warp_lag<R, FULL>(s, buf, xc, ph, local, base, len, shuffle_every, bad, hits);
+    if (MODE == 1) {
+      (void)run_chunk_warp_lag<R, FULL>(s, buf, xc, ph, local, base, len, shuffle_every, stall && sh_stall, bad,
+                                        hits);
+      stall = 0;
+    }
 #else
     if (MODE == 1) run_chunk_warp<R, FULL>(s, buf, local, base, len, shuffle_every, bad, hits);
 #endif

@@ -34,7 +34,7 @@ class Options(C.Structure):
                 ("threads_per_block", C.c_int), ("blocks", C.c_int), ("chain_samples", C.c_int),
                 ("seed_salt", C.c_uint64), ("de_tile", C.c_int), ("de_kernel", C.c_int),
                 ("de_stats", C.c_int), ("float_buckets", C.c_int), ("host_plan", C.c_int),
-                ("tail_chain_samples", C.c_int), ("tail_wave_pct", C.c_int), ("reserved", C.c_int * 1)]
+                ("tail_chain_samples", C.c_int), ("tail_wave_pct", C.c_int), ("test_exchange_stall", C.c_int)]
 
 
 class PngText(C.Structure):

@@ -347,6 +347,8 @@ const char *flam3gpu_version(void);
  * 2048-sample chains) run in chunks a quarter as long, so the blocks finish
  * close together; the chunking is fixed when a render is planned (the same
  * for the plain and the served render of a frame).
+ * test_exchange_stall: tests only (failure detection of the point
+ * exchange; no fault): see the field.
  * host_plan: 0 = the temporal samples of frames with several genomes
  * (animation, motion blur) are interpolated, prepared and packed on the
  * device, one block per sample; 1 = on host threads (always for one genome,
@@ -366,7 +368,8 @@ typedef struct {
   int host_plan;      /* 1: plan every temporal sample on host threads (0: multi-genome frames on the device) */
   int tail_chain_samples; /* samples per thread of the launch's last chunks (0: chain length / 4; -1: none) */
   int tail_wave_pct;  /* those chunks hold this percentage of one wave of full chunks (0: 50, 100 for 2048-sample chains) */
-  int reserved[1];
+  int test_exchange_stall; /* tests only: 1 makes one block of the next iterate launch withhold a point-exchange
+                              arrival, so its waits run out (20 ms) and the render fails with that error */
 } flam3gpu_options;
 
 void flam3gpu_default_options(flam3gpu_options *o);

@@ -210,3 +210,19 @@ def test_block_sizes_render_like_the_default(gpulib, hq_reference, threads, mode
         iters[t] = st.num_iters
     assert iters[threads] == iters[256]
     assert errs[threads] <= 1.05 * errs[256] + 0.03, errs
+
+
+def test_exchange_wait_runs_out_and_the_context_stays_usable(gpulib):
+    """Failure detection of the iterate kernel's point exchange, without a GPU
+    fault: with the test option one block withholds an mbarrier arrival, its
+    warps' bounded waits run out after 20 ms, the kernel sets its error flag
+    and the render fails with that error; the next render on the same context
+    succeeds."""
+    render.set_options(test_exchange_stall=1)
+    try:
+        with pytest.raises(render.Flam3GpuError, match="exchange wait timed out"):
+            render.render(gm.Frame(cfg0(q=50.0), bits=33, seed="stall"))
+    finally:
+        render.reset_options()
+    out, st = render.render(gm.Frame(cfg0(q=50.0), bits=33, seed="after-stall"))
+    assert out.mean() > 1.0 and st.num_iters > 0
