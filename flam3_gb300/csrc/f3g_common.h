@@ -151,8 +151,8 @@ typedef struct {
   unsigned long long badvals;     /* bad values and samples plotted, when a */
   unsigned long long plotted;     /* pass's counters point here */
   unsigned long long error;       /* nonzero: a kernel refused its input */
-  unsigned long long test_stall;  /* input, tests only: nonzero makes block 0 withhold one exchange
-                                     arrival and limits exchange waits to 20 ms */
+  unsigned long long test_stall;  /* input, tests only: 1 + c makes the block that runs chunk c withhold
+                                     one exchange arrival and limits its waits to 20 ms; 0: off */
 } F3GCounters;
 
 #endif

@@ -860,14 +860,13 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GI
   __shared__ int sh_item;
 #if F3G_EXCHANGE == 1
   __shared__ Exchange xc;
-  __shared__ int sh_stall;
+  __shared__ unsigned long long sh_stall; /* the stall test: 1 + the chunk that withholds, or 0 */
   unsigned ph = 0; /* phase parities of xc.bar[0..1] */
-  int stall = 1;   /* the stall test applies to block 0's first chunk only */
   if (MODE == 1 && threadIdx.x == 0) {
     mbar_init(&xc.bar[0], blockDim.x >> 5);
     mbar_init(&xc.bar[1], blockDim.x >> 5);
     xc.abort = 0;
-    sh_stall = blockIdx.x == 0 && ctr->test_stall != 0;
+    sh_stall = ctr->test_stall;
   }
 #endif
   int cur = -1;
@@ -923,11 +922,9 @@ __global__ void __launch_bounds__(256, IterMinBlocks<R>::v) k_iterate(const F3GI
       len = TT * s.S_tail;
     }
 #if F3G_EXCHANGE == 1
-    if (MODE == 1) {
-      (void)run_chunk_warp_lag<R, FULL>(s, buf, xc, ph, local, base, len, shuffle_every, stall && sh_stall, bad,
-                                        hits);
-      stall = 0;
-    }
+    if (MODE == 1)
+      (void)run_chunk_warp_lag<R, FULL>(s, buf, xc, ph, local, base, len, shuffle_every,
+                                        sh_stall != 0 && (unsigned long long)g == sh_stall - 1, bad, hits);
 #else
     if (MODE == 1) run_chunk_warp<R, FULL>(s, buf, local, base, len, shuffle_every, bad, hits);
 #endif

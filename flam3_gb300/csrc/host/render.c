@@ -959,7 +959,7 @@ int flam3gpu_render_ex(flam3_frame *spec, void *out, int field, int nchan, int t
         F3GCounters init;
         memset(&init, 0, sizeof(init));
         init.next_chunk = (unsigned long long)lo;
-        init.test_stall = f3g_opts.test_exchange_stall != 0;
+        init.test_stall = f3g_opts.test_exchange_stall ? (unsigned long long)lo + 1 : 0; /* the launch's first chunk */
         *c->h_ctr = init;
         CK(cudaMemcpyAsync(c->d_ctr, c->h_ctr, sizeof(F3GCounters), cudaMemcpyHostToDevice, c->stream));
         h2d += sizeof(F3GCounters);
