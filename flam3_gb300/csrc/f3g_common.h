@@ -152,7 +152,7 @@ typedef struct {
   unsigned long long plotted;     /* pass's counters point here */
   unsigned long long error;       /* nonzero: a kernel refused its input */
   unsigned long long test_stall;  /* input, tests only: 1 + c makes the block that runs chunk c withhold
-                                     one exchange arrival and limits its waits to 20 ms; 0: off */
+                                     one exchange arrival, so its waits run out (2 s); 0: off */
 } F3GCounters;
 
 #endif

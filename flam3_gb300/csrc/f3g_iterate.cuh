@@ -657,8 +657,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 /* waits for the completion of the barrier's phase of parity `ph`; false when
- * it has not completed within limit_ns (a lost arrival) */
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned ph, unsigned long long limit_ns) {
+ * it has not completed within about two seconds (a lost arrival) */
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned ph) {
   const unsigned a = smem_addr(bar);
   unsigned long long t0 = 0;
   for (unsigned i = 0; i < (1u << 30); i++) {
@@ -672,7 +672,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned ph, unsigned l
     if ((i & 255) == 0) {
       const unsigned long long t = global_ns();
       if (i == 0) t0 = t;
-      else if (t - t0 > limit_ns) return false;
+      else if (t - t0 > 2000000000ull) return false;
     }
   }
   return false;
@@ -745,7 +745,9 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     X[rslot] = ax; X[T + rslot] = ay; X[2 * T + rslot] = ac;
     reinterpret_cast<int *>(X + 3 * T)[rslot] = 0;
     __syncwarp();
-    if (lane == 0) mbar_arrive(&xc.bar[1]);
+    /* the stall test: warp 0 withholds this arrival, so every warp's first
+     * wait runs out */
+    if (lane == 0 && !(stall && wl == 0)) mbar_arrive(&xc.bar[1]);
   }
   int fuse_left = 2 * s.fuse + shuffle_every;
 #if !F3G_ROT_CLOSED
@@ -773,8 +775,7 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     const int cur = round & 1, prev = cur ^ 1;
     /* the points of round h-1 (the warp decides together, so a wait that
      * ends at the time limit in one lane ends the exchange for all) */
-    /* every wait ends within 2 s (20 ms in the stall test) */
-    if (!__all_sync(0xffffffffu, mbar_wait(&xc.bar[prev], (ph >> prev) & 1u, stall ? 20000000ull : 2000000000ull))) {
+    if (!__all_sync(0xffffffffu, mbar_wait(&xc.bar[prev], (ph >> prev) & 1u))) {
       xc.abort = 1;
       ok_all = false;
       break;
@@ -804,9 +805,7 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     reinterpret_cast<int *>(W + 3 * T)[wslot] = consec;
     const unsigned ndone = __popc(__ballot_sync(0xffffffffu, remaining == 0 && fuse_left == 0));
     __syncwarp();
-    /* the stall test: warp 0 withholds its arrival of round 2, so every
-     * warp's wait for that round runs out */
-    if (lane == 0 && !(stall && wl == 0 && round == 2)) {
+    if (lane == 0) {
       if (ndone) atomicAdd(&xc.done[round & 3], (int)ndone);
       mbar_arrive(&xc.bar[cur]);
     }

@@ -369,7 +369,7 @@ typedef struct {
   int tail_chain_samples; /* samples per thread of the launch's last chunks (0: chain length / 4; -1: none) */
   int tail_wave_pct;  /* those chunks hold this percentage of one wave of full chunks (0: 50, 100 for 2048-sample chains) */
   int test_exchange_stall; /* tests only: 1 makes one block of the next iterate launch withhold a point-exchange
-                              arrival, so its waits run out (20 ms) and the render fails with that error */
+                              arrival, so its waits run out (2 s) and the render fails with that error */
 } flam3gpu_options;
 
 void flam3gpu_default_options(flam3gpu_options *o);

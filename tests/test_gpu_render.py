@@ -215,7 +215,7 @@ def test_block_sizes_render_like_the_default(gpulib, hq_reference, threads, mode
 def test_exchange_wait_runs_out_and_the_context_stays_usable(gpulib):
     """Failure detection of the iterate kernel's point exchange, without a GPU
     fault: with the test option one block withholds an mbarrier arrival, its
-    warps' bounded waits run out after 20 ms, the kernel sets its error flag
+    warps' bounded waits run out after 2 s, the kernel sets its error flag
     and the render fails with that error; the next render on the same context
     succeeds."""
     render.set_options(test_exchange_stall=1)
