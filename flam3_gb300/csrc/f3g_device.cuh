@@ -156,19 +156,11 @@ __device__ __forceinline__ float m_atan2(float y, float x) {
   return copysignf(r, y);
 }
 /* square root: the hardware approximation (PTX sqrt.approx.f32: one
- * instruction, 0 for 0, NaN below 0); F3G_SQRT_RSQ keeps x * rsqrt(x) with
- * the zero and negative cases selected (about 3 ulp) */
-#ifndef F3G_SQRT_RSQ
-#define F3G_SQRT_RSQ 0
-#endif
+ * instruction, 0 for 0, NaN below 0) */
 __device__ __forceinline__ float m_sqrt(float x) {
-#if F3G_SQRT_RSQ
-  return x > 0.0f ? x * rsqrtf(x) : (x == 0.0f ? 0.0f : __int_as_float(0x7fc00000));
-#else
   float r;
   asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
-#endif
 }
 #else
 __device__ __forceinline__ float m_atan2(float y, float x) { return atan2f(y, x); }
@@ -206,18 +198,9 @@ __device__ __forceinline__ double m_fabs(double x) { return fabs(x); }
 #define F3G_ANGLES_RSQ 1
 #endif
 
-/* NaN, or |x| > 1e10 (flam3.c:269-272); the one-compare form measured
- * 1.1 % faster on the 1920x1080 still (48.9 against 48.3 Giter/s) */
-#ifndef F3G_BADVAL_ABS
-#define F3G_BADVAL_ABS 1
-#endif
-template <typename R> __device__ __forceinline__ bool badvalue(R x) {
-#if F3G_BADVAL_ABS
-  return !(fabs(x) <= (R)1e10); /* one compare of |x|, false for NaN */
-#else
-  return (x != x) || (x > (R)1e10) || (x < (R)-1e10);
-#endif
-}
+/* NaN, or |x| > 1e10 (flam3.c:269-272), as one compare of |x| (false for
+ * NaN) */
+template <typename R> __device__ __forceinline__ bool badvalue(R x) { return !(fabs(x) <= (R)1e10); }
 
 /* One xform staged in shared memory in the iteration precision. */
 /* 16-byte aligned: apply_xform loads its FP32 fields as vectors */

@@ -487,17 +487,10 @@ __device__ __forceinline__ int group_or(int id, int n, int pred) {
   return r;
 }
 
-/* F3G_WW_ROTATE (off): measured 0.4 % faster alone but 0.4 % slower than
- * off together with the one-compare bad-value test on the 1920x1080 still */
-#ifndef F3G_WW_ROTATE
-#define F3G_WW_ROTATE 0
-#endif
 /* Warp-shared stream of xform-choice words: lane L holds four words of the
  * current 128-word block of counter (chunk, block, 0xC0DE0000 | warp, L),
- * so one Philox call per lane serves 128 steps of the warp; with
- * F3G_WW_ROTATE word k is component k / 32 of lane k % 32 (one shuffle from
- * the same register every step), else component k % 4 of lane k / 4.  The
- * counters are disjoint
+ * so one Philox call per lane serves 128 steps of the warp; word k is
+ * component k % 4 of lane k / 4 (one shuffle).  The counters are disjoint
  * from the per-thread streams (third word = thread index < 0xC0DE0000). */
 struct WarpWords {
   uint4 blk;
@@ -506,28 +499,16 @@ struct WarpWords {
   __device__ __forceinline__ void init(uint32_t key0, uint32_t key1, uint32_t chunk, uint32_t warp, uint32_t ln) {
     k0 = key0; k1 = key1; c0 = chunk; next = 0; tag = 0xC0DE0000u | warp; lane = ln; used = 128;
   }
-  /* warp-uniform: every lane of the warp calls it at the same step; word
-   * 32m + i of a block is component m of lane i's four words, and the
-   * components move down one place every 32 words, so each step shuffles
-   * from the same register */
+  /* warp-uniform: every lane of the warp calls it at the same step */
   __device__ __forceinline__ uint32_t word() {
     if (used == 128) {
       blk = philox_block(c0, next, tag, lane, k0, k1);
       next++;
       used = 0;
     }
-#if F3G_WW_ROTATE
-    else if ((used & 31) == 0) {
-      blk.x = blk.y;
-      blk.y = blk.z;
-      blk.z = blk.w;
-    }
-    const uint32_t w = __shfl_sync(0xffffffffu, blk.x, used & 31);
-#else
     const int c = used & 3;
     const uint32_t mine = c == 0 ? blk.x : c == 1 ? blk.y : c == 2 ? blk.z : blk.w;
     const uint32_t w = __shfl_sync(0xffffffffu, mine, used >> 2);
-#endif
     used++;
     return w;
   }
@@ -634,12 +615,6 @@ __device__ void run_chunk_warp(const PassS<R> &s, ShufPoint<R> *buf, long long l
  *      round apart instead of meeting every round. */
 #ifndef F3G_EXCHANGE
 #define F3G_EXCHANGE 1
-#endif
-
-/* F3G_ROT_CLOSED: the exchange's round rotation from the round number
- * (1) or accumulated across rounds (0) -- the same values */
-#ifndef F3G_ROT_CLOSED
-#define F3G_ROT_CLOSED 0
 #endif
 
 /* shared-memory mbarrier helpers (PTX mbarrier.*; CTA scope) */
@@ -750,9 +725,7 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     if (lane == 0 && !(stall && wl == 0)) mbar_arrive(&xc.bar[1]);
   }
   int fuse_left = 2 * s.fuse + shuffle_every;
-#if !F3G_ROT_CLOSED
-  uint32_t rot_acc = 0;
-#endif
+  uint32_t rot_acc = 0; /* the rounds' rotation, accumulated */
   /* bucket-sharing probes: bits 0-2 probes taken, 3-5 probes with shared
    * buckets, bit 6 aggregation on */
   int agg_state = (F3G_AGG == 2 || (F3G_AGG == 1 && s.bucket_kind == F3G_BK_F64)) ? 64 : 0;
@@ -789,14 +762,8 @@ __device__ bool run_chunk_warp_lag(const PassS<R> &s, ShufPoint<R> *buf, Exchang
     /* this round's points to buffer h&1: transpose lanes across warps, XOR
      * the low five bits, rotate by whole 32-point segments (block-uniform
      * amounts), at swizzled slots (32 distinct banks) */
-    /* 0x9E3779B1 * (1 + 2 + ... + (h+1)), from the round (no register
-     * carried across rounds) */
-#if F3G_ROT_CLOSED
-    const uint32_t rot = 0x9E3779B1u * (((uint32_t)(round + 1) * (uint32_t)(round + 2)) >> 1);
-#else
     rot_acc += 0x9E3779B1u * (uint32_t)(round + 1);
     const uint32_t rot = rot_acc;
-#endif
     const int x5 = (int)(rot >> 27), kr = (int)(rot >> 24) % G;
     const int dst = (((lane * G + wl) ^ x5) + 32 * kr) & (T - 1);
     const int wslot = dst ^ ((dst >> 5) & 31);
