@@ -192,10 +192,14 @@ __device__ __forceinline__ double m_fabs(double x) { return fabs(x); }
 #define F3G_LAZY_ANGLES 1
 #endif
 
-/* F3G_ANGLES_RSQ: FP32 sin and cos of the angle (x/r, y/r) from one
- * reciprocal square root instead of two approximate divides */
+/* F3G_ANGLES_RSQ (with the fast FP32 math): FP32 sin and cos of the angle
+ * (x/r, y/r) from one reciprocal square root instead of two divides */
 #ifndef F3G_ANGLES_RSQ
+#ifdef F3G_FAST_MATH
 #define F3G_ANGLES_RSQ 1
+#else
+#define F3G_ANGLES_RSQ 0
+#endif
 #endif
 
 /* NaN, or |x| > 1e10 (flam3.c:269-272), as one compare of |x| (false for
