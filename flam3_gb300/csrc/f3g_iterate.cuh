@@ -4,19 +4,22 @@
  * Replaces iter_thread (rect.c:253-527), flam3_iterate (flam3.c:232-299) and
  * the bucket accumulation (rect.c:411-516).  One persistent launch processes
  * any number of passes (temporal samples, frames, jobs): work is cut into
- * chunks of blockDim*S samples; a block takes chunk indices from a global
- * counter, stages the chunk's pass (xforms, variation lists, xform-choice
- * breakpoints, colour map, camera) in shared memory, and runs fresh chains:
- * random start point, `fuse` discarded steps, then S samples per thread.
+ * chunks of blockDim*S samples (blockDim*S_tail from a pass's chunk_tail on:
+ * the short chunks that end a launch); a block takes chunk indices from a
+ * global counter, stages the chunk's pass (xforms, variation lists,
+ * xform-choice breakpoints, colour map, camera) in shared memory, and runs
+ * fresh chains: random start point, discarded fuse steps, then its samples.
  *
  * Two ways to pick xforms:
  *   mode 0: every thread draws its own xform per step (the reference's
- *           semantics, and the only mode for genomes with xaos);
+ *           semantics, and the only mode for genomes with xaos and for
+ *           blocks of fewer than 4 warps);
  *   mode 1: one draw per warp per step, so the 32 lanes run the same
- *           variation code; every `shuffle_every` steps the block permutes
- *           its points through shared memory so the lanes of a warp hold
- *           points with different histories.  Each point still sees an
- *           i.i.d. xform sequence with the genome's probabilities.
+ *           variation code; every `shuffle_every` steps the warps exchange
+ *           their points through shared memory (lagged by a round, on
+ *           mbarriers: F3G_EXCHANGE) so the lanes of a warp hold points
+ *           with different histories.  Each point still sees an i.i.d.
+ *           xform sequence with the genome's probabilities.
  *
  * Samples are added to float4 buckets with one vector atomic
  * (red.global.add.v4.f32) or to double buckets with four FP64 atomics.
