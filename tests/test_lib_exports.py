@@ -90,3 +90,25 @@ def test_analysis_helpers_need_a_random_context():
     assert lib.flam3gpu_dimension(C.byref(G.g), 1000, 0, None) == -1.0
     assert b"ISAAC" in lib.flam3gpu_last_error()
     assert lib.flam3gpu_lyapunov(C.byref(G.g), 10, None) == -1.0
+
+
+def test_struct_mirrors_match_the_library_without_gpu():
+    """The Python mirrors of flam3gpu_options and flam3gpu_service_config are
+    at least as large as the library's structs (its default writers stop
+    inside them: canary bytes after the mirror stay untouched) and the
+    defaults land in the mirrored fields."""
+    from flam3_gb300 import render, service
+
+    lib = render.load()
+    for cls, fill in ((render.Options, lib.flam3gpu_default_options),
+                      (service.ServiceConfig, service._lib().flam3gpu_service_default_config)):
+        n = C.sizeof(cls)
+        buf = (C.c_ubyte * (n + 64))(*([0xAB] * (n + 64)))
+        fill(C.cast(buf, C.POINTER(cls)))
+        assert bytes(buf[n:]) == b"\xab" * 64, cls.__name__
+    o = render.Options()
+    lib.flam3gpu_default_options(C.byref(o))
+    assert (o.shuffle_every, o.chain_samples, o.tail_chain_samples, o.tail_wave_pct, o.test_exchange_stall) == \
+        (3, 0, 0, 0, 0)
+    c = service.config()
+    assert c.order == 1 and c.max_inflight == 2
