@@ -112,3 +112,12 @@ def test_struct_mirrors_match_the_library_without_gpu():
         (3, 0, 0, 0, 0)
     c = service.config()
     assert c.order == 1 and c.max_inflight == 2
+
+
+def test_pass_record_mirror_without_gpu():
+    """The tests' ctypes mirror of the iterate kernel's pass record has the
+    library's size (flam3gpu_pass_bytes is host code)."""
+    from flam3_gb300 import render
+    from test_gpu_plan import F3GPass
+
+    assert C.sizeof(F3GPass) == render.load().flam3gpu_pass_bytes()
